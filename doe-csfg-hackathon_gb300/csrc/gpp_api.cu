@@ -1,0 +1,588 @@
+// gpp_api.cu -- the C ABI of libgpp_gb300.so (include/gpp_gb300.h): argument
+// validation, workspace, kernel dispatch, the deterministic reduction plan,
+// streams, error reporting and the host-buffer (end-to-end) path.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+#include <chrono>
+
+#include "gpp_gb300.h"
+#include "gpp_kernels.h"
+
+namespace gpp {
+
+namespace {
+thread_local std::string t_err;
+thread_local unsigned long long t_launches = 0;
+thread_local cudaStream_t t_compat_stream = nullptr;
+thread_local bool t_timing = false;
+thread_local cudaEvent_t t_ev0 = nullptr, t_ev1 = nullptr;
+thread_local bool t_timed = false;
+}  // namespace
+
+void count_launch(int n) { t_launches += (unsigned long long)n; }
+
+namespace {
+
+gpp_status fail(gpp_status s, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_err = buf;
+    return s;
+}
+
+gpp_status cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(GPP_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(GPP_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GPP_CUDA_TRY(call, what)                          \
+    do {                                                  \
+        cudaError_t e_ = (call);                          \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+// One persistent fault word per device (allocated on first use).
+std::mutex g_dev_mutex;
+int *g_err_word[256] = {};
+bool g_pool_ready[256] = {};
+
+gpp_status device_setup(int *dev_out, int **err_out) {
+    int dev = 0;
+    GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= 256) return fail(GPP_ERR_UNSUPPORTED, "device ordinal %d", dev);
+    std::lock_guard<std::mutex> lk(g_dev_mutex);
+    if (!g_err_word[dev]) {
+        int *w = nullptr;
+        GPP_CUDA_TRY(cudaMalloc(&w, sizeof(int)), "cudaMalloc(fault word)");
+        GPP_CUDA_TRY(cudaMemset(w, 0, sizeof(int)), "cudaMemset(fault word)");
+        g_err_word[dev] = w;
+    }
+    if (!g_pool_ready[dev]) {
+        // Keep stream-ordered workspace allocations cached between calls.
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            unsigned long long thr = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        }
+        g_pool_ready[dev] = true;
+    }
+    *dev_out = dev;
+    *err_out = g_err_word[dev];
+    return GPP_OK;
+}
+
+bool mul_ok(long long a, long long b, long long lim) { return a == 0 || b <= lim / a; }
+
+gpp_status validate(const gpp_problem *pr) {
+    if (!pr) return fail(GPP_ERR_INVALID_ARGUMENT, "problem is NULL");
+    const gpp_problem &p = *pr;
+    if (p.number_bands < 0 || p.nvband < 0 || p.nvband > p.number_bands)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "need 0 <= nvband <= number_bands (got %d, %d)",
+                    p.nvband, p.number_bands);
+    if (p.ncouls <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ncouls must be > 0 (got %d)", p.ncouls);
+    if (p.ngpown < 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ngpown must be >= 0 (got %d)", p.ngpown);
+    if (p.nw <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "nw must be > 0 (got %d)", p.nw);
+    if (p.wx_stride != 0 && p.wx_stride < p.nw)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "wx_stride must be 0 or >= nw (got %d)", p.wx_stride);
+    if (p.semantics != GPP_SEM_COMPLEX_SEQ && p.semantics != GPP_SEM_KERSEQ)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown semantics %d", p.semantics);
+    if (p.precision != GPP_PRECISION_FP64 && p.precision != GPP_PRECISION_MIXED)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown precision %d", p.precision);
+    const long long lim = (long long)1 << 60;
+    if (!mul_ok(p.number_bands, p.ncouls, lim) || !mul_ok(p.ngpown, p.ncouls, lim) ||
+        !mul_ok((long long)p.number_bands * (p.wx_stride ? 1 : 0), p.wx_stride ? p.wx_stride : 1, lim))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "array sizes overflow");
+    if (p.number_bands > 0 && (!p.aqsmtemp || !p.aqsntemp))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "aqsmtemp/aqsntemp is NULL");
+    if (p.ngpown > 0 && (!p.I_eps_array || !p.wtilde_array || !p.inv_igp_index))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "I_eps_array/wtilde_array/inv_igp_index is NULL");
+    if (!p.vcoul || !p.wx_array) return fail(GPP_ERR_INVALID_ARGUMENT, "vcoul/wx_array is NULL");
+    return GPP_OK;
+}
+
+Problem to_problem(const gpp_problem &q) {
+    Problem p;
+    p.aqsm = reinterpret_cast<const double2 *>(q.aqsmtemp);
+    p.aqsn = reinterpret_cast<const double2 *>(q.aqsntemp);
+    p.ieps = reinterpret_cast<const double2 *>(q.I_eps_array);
+    p.wt = reinterpret_cast<const double2 *>(q.wtilde_array);
+    p.vcoul = q.vcoul;
+    p.inv_igp = q.inv_igp_index;
+    p.indinv = q.indinv;
+    p.wx = q.wx_array;
+    p.wx_stride = q.wx_stride;
+    p.nb = q.number_bands;
+    p.nv = q.nvband;
+    p.nc = q.ncouls;
+    p.ng = q.ngpown;
+    p.nw = q.nw;
+    p.occ = q.occ;
+    p.semantics = q.semantics;
+    return p;
+}
+
+// Where the final fixed-order sums go.
+struct OutSpec {
+    double2 *ach = nullptr;  // [nw] complex (overwrite or accumulate)
+    double *ach_re = nullptr, *ach_im = nullptr;  // split, accumulate
+    double2 *asx = nullptr;  // [nw]
+    double2 *n1 = nullptr;   // [nb] indexed by absolute band
+    double2 *achs = nullptr; // [1]
+    double *achs_re = nullptr, *achs_im = nullptr;
+    int accumulate = 0;
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Runs the bands [b0, b1) of problem p: occupied bands (< nv) through the
+// flag kernel, the rest through the FP64 or mixed unoccupied kernel, then
+// reduces all block partials in a fixed order into the outputs.
+gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutSpec &o,
+                     bool do_main, cudaStream_t s) {
+    int dev = 0;
+    int *err = nullptr;
+    gpp_status st = device_setup(&dev, &err);
+    if (st != GPP_OK) return st;
+
+    const int fb0 = b0, fb1 = do_main ? (b1 < p.nv ? b1 : p.nv) : b0;
+    const int nb0 = do_main ? (b0 > p.nv ? b0 : p.nv) : b1, nb1 = b1;
+    const bool has_flag = fb1 > fb0 && p.ng > 0;
+    const bool has_noflag = nb1 > nb0 && p.ng > 0;
+    const bool mixed = precision == GPP_PRECISION_MIXED && has_noflag;
+
+    const TileShape fs = flag_shape(p);
+    const TileShape ns = mixed ? mixed_noflag_shape(p) : fp64_noflag_shape(p);
+    const long long rows_f = has_flag ? ceil_div(p.ng, fs.rg) : 0;
+    const long long rows_n = has_noflag ? ceil_div(p.ng, ns.rg) : 0;
+    const long long tiles_f = has_flag ? rows_f * (fb1 - fb0) : 0;
+    const long long tiles_n = has_noflag ? rows_n * ceil_div(nb1 - nb0, ns.rn) : 0;
+    if (has_noflag && ceil_div(nb1 - nb0, ns.rn) > 65535)
+        return fail(GPP_ERR_UNSUPPORTED, "too many bands for one launch (%d)", nb1 - nb0);
+    if (ceil_div(p.nw, ns.nwc) > 65535 || (has_flag && fb1 - fb0 > 65535))
+        return fail(GPP_ERR_UNSUPPORTED, "too many frequencies or occupied bands");
+    if (has_flag && fb0 != 0)
+        return fail(GPP_ERR_UNSUPPORTED, "occupied-band launches start at band 0");
+    const long long ach_seg = tiles_f + tiles_n;
+    const long long n1_seg = rows_f > rows_n ? rows_f : rows_n;
+    const bool want_n1 = o.n1 && p.nw >= 3 && p.ng > 0;
+    const bool want_achs = (o.achs || o.achs_re) && p.ng > 0 && b1 > b0;
+    const int achs_blocks = want_achs ? achstemp_blocks(p) : 0;
+
+    size_t off = 0;
+    const size_t o_ach = off; off = align_up(off + sizeof(double2) * (size_t)(ach_seg * p.nw));
+    const size_t o_asx = off; off = align_up(off + sizeof(double2) * (size_t)(tiles_f * p.nw));
+    const size_t o_n1 = off; off = align_up(off + (want_n1 ? sizeof(double2) * (size_t)(n1_seg * p.nb) : 0));
+    const size_t o_st = off; off = align_up(off + sizeof(double2) * (size_t)achs_blocks);
+    const size_t o_split = off; off = align_up(off + (mixed ? mixed_split_bytes(p) : 0));
+    const size_t ws_bytes = off > 0 ? off : 256;
+
+    void *ws = nullptr;
+    GPP_CUDA_TRY(cudaMallocAsync(&ws, ws_bytes, s), "cudaMallocAsync(workspace)");
+    char *w = static_cast<char *>(ws);
+
+    Partials part{};
+    part.ach = reinterpret_cast<double2 *>(w + o_ach);
+    part.ach_seg = ach_seg;
+    part.asx = reinterpret_cast<double2 *>(w + o_asx);
+    part.asx_seg = tiles_f;
+    part.n1 = want_n1 ? reinterpret_cast<double2 *>(w + o_n1) : nullptr;
+    part.n1_seg = (int)n1_seg;
+    part.err = err;
+
+    cudaError_t e = cudaSuccess;
+    if (want_n1 && (rows_f != rows_n) && has_flag && has_noflag) {
+        // Different row tilings: pad the shorter per-band segments with zeros.
+        e = cudaMemsetAsync(part.n1, 0, sizeof(double2) * (size_t)(n1_seg * p.nb), s);
+    }
+    if (e == cudaSuccess && has_flag) {
+        part.ach_tile0 = 0;
+        e = launch_flag_fp64(p, part, s);
+    }
+    if (e == cudaSuccess && has_noflag) {
+        part.ach_tile0 = (int)tiles_f;
+        if (t_timing && t_ev0) cudaEventRecord(t_ev0, s);
+        e = mixed ? launch_mixed_noflag(p, part, w + o_split, nb0, nb1, s)
+                  : launch_noflag_fp64(p, part, nb0, nb1, s);
+        if (t_timing && t_ev1) {
+            cudaEventRecord(t_ev1, s);
+            t_timed = true;
+        }
+    }
+    if (e == cudaSuccess && want_achs)
+        e = launch_achstemp(p, reinterpret_cast<double2 *>(w + o_st), err, s);
+
+    // Fixed-order reduction of the block partials.
+    if (e == cudaSuccess && (o.ach || o.ach_re)) {
+        ReduceOut ro{o.ach, o.ach_re, o.ach_im, o.accumulate};
+        e = launch_reduce(part.ach, ach_seg, (int)ach_seg, p.nw, ro, s);
+    }
+    if (e == cudaSuccess && o.asx) {
+        ReduceOut ro{o.asx, nullptr, nullptr, o.accumulate};
+        e = launch_reduce(part.asx, tiles_f, (int)tiles_f, p.nw, ro, s);
+    }
+    if (e == cudaSuccess && want_n1 && b1 > b0) {
+        ReduceOut ro{o.n1 + b0, nullptr, nullptr, o.accumulate};
+        e = launch_reduce(part.n1 + (size_t)b0 * n1_seg, n1_seg, (int)n1_seg, b1 - b0, ro, s);
+    }
+    if (e == cudaSuccess && want_achs) {
+        ReduceOut ro{o.achs, o.achs_re, o.achs_im, o.accumulate};
+        e = launch_reduce(reinterpret_cast<double2 *>(w + o_st), achs_blocks, achs_blocks, 1, ro, s);
+    }
+    cudaError_t e2 = cudaFreeAsync(ws, s);
+    if (e != cudaSuccess) return cuda_fail(e, "kernel launch");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFreeAsync(workspace)");
+    return GPP_OK;
+}
+
+}  // namespace
+}  // namespace gpp
+
+using namespace gpp;
+
+extern "C" {
+
+const char *gpp_last_error_message(void) { return t_err.c_str(); }
+unsigned long long gpp_launch_count(void) { return t_launches; }
+void gpp_reset_launch_count(void) { t_launches = 0; }
+
+gpp_status gpp_set_stream(gpp_stream_t stream) {
+    t_compat_stream = reinterpret_cast<cudaStream_t>(stream);
+    return GPP_OK;
+}
+gpp_stream_t gpp_get_stream(void) { return reinterpret_cast<gpp_stream_t>(t_compat_stream); }
+
+gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_stream_t stream) {
+    gpp_status st = validate(problem);
+    if (st != GPP_OK) return st;
+    if (!out || !out->achtemp || !out->asxtemp)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "outputs achtemp/asxtemp are required");
+    if (out->acht_n1_loc && problem->nw < 3)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "acht_n1_loc needs nw >= 3 (it sums the iw = 2 column)");
+    Problem p = to_problem(*problem);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    OutSpec o;
+    o.ach = reinterpret_cast<double2 *>(out->achtemp);
+    o.asx = reinterpret_cast<double2 *>(out->asxtemp);
+    o.n1 = reinterpret_cast<double2 *>(out->acht_n1_loc);
+    o.achs = reinterpret_cast<double2 *>(out->achstemp);
+    o.accumulate = 0;
+    if (o.n1 && (p.nb == 0 || p.ng == 0)) {
+        cudaError_t e = cudaMemsetAsync(o.n1, 0, sizeof(double2) * (size_t)p.nb, s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(acht_n1_loc)");
+    }
+    if (o.achs && (p.nb == 0 || p.ng == 0)) {
+        cudaError_t e = cudaMemsetAsync(o.achs, 0, sizeof(double2), s);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(achstemp)");
+    }
+    return run_sigma(p, 0, p.nb, problem->precision, o, true, s);
+}
+
+gpp_status gpp_kernel_gpu(const gpp_complex *wtilde_array, const gpp_complex *aqsntemp,
+                          const gpp_complex *aqsmtemp, const gpp_complex *I_eps_array, int ncouls,
+                          int ngpown, int number_bands, const double *wx_array, double *achtemp_re,
+                          double *achtemp_im, const double *vcoul, int nstart, int nend,
+                          const int *indinv, const int *inv_igp_index) {
+    gpp_problem q{};
+    q.number_bands = number_bands;
+    q.nvband = 0;
+    q.ncouls = ncouls;
+    q.ngpown = ngpown;
+    q.nw = nend - nstart;
+    q.aqsmtemp = aqsmtemp;
+    q.aqsntemp = aqsntemp;
+    q.I_eps_array = I_eps_array;
+    q.wtilde_array = wtilde_array;
+    q.vcoul = vcoul;
+    q.inv_igp_index = inv_igp_index;
+    q.indinv = indinv;
+    q.wx_array = wx_array;
+    q.wx_stride = 0;
+    q.occ = 1.0;
+    q.semantics = GPP_SEM_COMPLEX_SEQ;
+    q.precision = GPP_PRECISION_FP64;
+    gpp_status st = validate(&q);
+    if (st != GPP_OK) return st;
+    if (!achtemp_re || !achtemp_im) return fail(GPP_ERR_INVALID_ARGUMENT, "achtemp_re/im is NULL");
+    OutSpec o;
+    o.ach_re = achtemp_re;
+    o.ach_im = achtemp_im;
+    o.accumulate = 1;
+    return run_sigma(to_problem(q), 0, number_bands, GPP_PRECISION_FP64, o, true, t_compat_stream);
+}
+
+static gpp_problem compat_problem(int number_bands, int nvband, int ngpown, int ncouls,
+                                  const int *inv_igp_index, const double *wx_array,
+                                  const gpp_complex *wtilde_array, const gpp_complex *aqsmtemp,
+                                  const gpp_complex *aqsntemp, const gpp_complex *I_eps_array,
+                                  const double *vcoul, double occ) {
+    gpp_problem q{};
+    q.number_bands = number_bands;
+    q.nvband = nvband;
+    q.ncouls = ncouls;
+    q.ngpown = ngpown;
+    q.nw = 3;  // nstart = 0, nend = 3 (GPPComplex.cu:2-3)
+    q.aqsmtemp = aqsmtemp;
+    q.aqsntemp = aqsntemp;
+    q.I_eps_array = I_eps_array;
+    q.wtilde_array = wtilde_array;
+    q.vcoul = vcoul;
+    q.inv_igp_index = inv_igp_index;
+    q.wx_array = wx_array;
+    q.wx_stride = 0;
+    q.occ = occ;
+    q.semantics = GPP_SEM_COMPLEX_SEQ;
+    q.precision = GPP_PRECISION_FP64;
+    return q;
+}
+
+gpp_status gpp_till_nvband(int nvband, int ngpown, int ncouls, const int *inv_igp_index,
+                           const double *wx_array, const gpp_complex *wtilde_array,
+                           const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                           const gpp_complex *I_eps_array, gpp_complex *asxtemp, const double *vcoul,
+                           gpp_complex *acht_n1_loc, double *achtemp_re, double *achtemp_im,
+                           double occ) {
+    gpp_problem q = compat_problem(nvband, nvband, ngpown, ncouls, inv_igp_index, wx_array,
+                                   wtilde_array, aqsmtemp, aqsntemp, I_eps_array, vcoul, occ);
+    gpp_status st = validate(&q);
+    if (st != GPP_OK) return st;
+    if (!achtemp_re || !achtemp_im || !asxtemp)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "achtemp_re/achtemp_im/asxtemp is NULL");
+    OutSpec o;
+    o.ach_re = achtemp_re;
+    o.ach_im = achtemp_im;
+    o.asx = reinterpret_cast<double2 *>(asxtemp);
+    o.n1 = reinterpret_cast<double2 *>(acht_n1_loc);
+    o.accumulate = 1;
+    return run_sigma(to_problem(q), 0, nvband, GPP_PRECISION_FP64, o, true, t_compat_stream);
+}
+
+gpp_status gpp_noflag_occ_solver(int number_bands, int nvband, int ngpown, int ncouls,
+                                 const int *inv_igp_index, const double *wx_array,
+                                 const gpp_complex *wtilde_array, const gpp_complex *aqsmtemp,
+                                 const gpp_complex *aqsntemp, const gpp_complex *I_eps_array,
+                                 const double *vcoul, double *achtemp_re, double *achtemp_im,
+                                 gpp_complex *acht_n1_loc) {
+    gpp_problem q = compat_problem(number_bands, nvband, ngpown, ncouls, inv_igp_index, wx_array,
+                                   wtilde_array, aqsmtemp, aqsntemp, I_eps_array, vcoul, 1.0);
+    gpp_status st = validate(&q);
+    if (st != GPP_OK) return st;
+    if (!achtemp_re || !achtemp_im) return fail(GPP_ERR_INVALID_ARGUMENT, "achtemp_re/im is NULL");
+    OutSpec o;
+    o.ach_re = achtemp_re;
+    o.ach_im = achtemp_im;
+    o.n1 = reinterpret_cast<double2 *>(acht_n1_loc);
+    o.accumulate = 1;
+    return run_sigma(to_problem(q), nvband, number_bands, GPP_PRECISION_FP64, o, true,
+                     t_compat_stream);
+}
+
+static gpp_status reduce_achstemp_impl(int number_bands, const int *inv_igp_index, int ncouls,
+                                       const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                                       const gpp_complex *I_eps_array, int ngpown,
+                                       const double *vcoul, OutSpec o) {
+    static const double dummy_wx = 0.0;  // the static term has no frequency
+    gpp_problem q = compat_problem(number_bands, 0, ngpown, ncouls, inv_igp_index, &dummy_wx,
+                                   I_eps_array, aqsmtemp, aqsntemp, I_eps_array, vcoul, 1.0);
+    gpp_status st = validate(&q);
+    if (st != GPP_OK) return st;
+    o.accumulate = 1;
+    return run_sigma(to_problem(q), 0, number_bands, GPP_PRECISION_FP64, o, false, t_compat_stream);
+}
+
+gpp_status gpp_reduce_achstemp(int number_bands, const int *inv_igp_index, int ncouls,
+                               const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                               const gpp_complex *I_eps_array, gpp_complex *achstemp, int ngpown,
+                               const double *vcoul) {
+    if (!achstemp) return fail(GPP_ERR_INVALID_ARGUMENT, "achstemp is NULL");
+    OutSpec o;
+    o.achs = reinterpret_cast<double2 *>(achstemp);
+    return reduce_achstemp_impl(number_bands, inv_igp_index, ncouls, aqsmtemp, aqsntemp,
+                                I_eps_array, ngpown, vcoul, o);
+}
+
+// Split real/imaginary destination, for the reference's d_reduce_achstemp
+// signature (GPPComplex.h:308); used by gpp_compat.cpp.
+gpp_status gpp_reduce_achstemp_split(int number_bands, const int *inv_igp_index, int ncouls,
+                                     const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                                     const gpp_complex *I_eps_array, double *re, double *im,
+                                     int ngpown, const double *vcoul) {
+    if (!re || !im) return fail(GPP_ERR_INVALID_ARGUMENT, "achstemp_re/im is NULL");
+    OutSpec o;
+    o.achs_re = re;
+    o.achs_im = im;
+    return reduce_achstemp_impl(number_bands, inv_igp_index, ncouls, aqsmtemp, aqsntemp,
+                                I_eps_array, ngpown, vcoul, o);
+}
+
+gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms) {
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t q = cudaStreamQuery(s);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) return cuda_fail(q, "cudaStreamQuery");
+        if (timeout_ms >= 0) {
+            auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+                          std::chrono::steady_clock::now() - t0).count();
+            if (ms >= timeout_ms) return fail(GPP_ERR_NOT_READY, "stream still busy after %d ms", timeout_ms);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    int dev = 0;
+    int *err = nullptr;
+    gpp_status st = device_setup(&dev, &err);
+    if (st != GPP_OK) return st;
+    int h = 0;
+    GPP_CUDA_TRY(cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost), "read fault word");
+    if (h) {
+        GPP_CUDA_TRY(cudaMemset(err, 0, sizeof(int)), "clear fault word");
+        return fail(GPP_ERR_BAD_INDEX, "device saw %s%s",
+                    (h & kErrBadIgp) ? "inv_igp_index < 0 " : "",
+                    (h & kErrBadIndinv) ? "indinv out of [0, ncouls)" : "");
+    }
+    return GPP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host-buffer path: a context owns device copies of the inputs and outputs.
+struct gpp_context {
+    cudaStream_t stream = nullptr;
+    void *dev = nullptr;
+    size_t dev_bytes = 0;
+    int device = 0;
+};
+
+gpp_status gpp_context_create(gpp_context **ctx) {
+    if (!ctx) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    gpp_context *c = new gpp_context();
+    cudaError_t e = cudaGetDevice(&c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_fail(e, "gpp_context_create");
+    }
+    *ctx = c;
+    return GPP_OK;
+}
+
+gpp_status gpp_context_destroy(gpp_context *ctx) {
+    if (!ctx) return GPP_OK;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->dev) cudaFree(ctx->dev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GPP_OK;
+}
+
+gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gpp_outputs *out) {
+    if (!ctx) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    gpp_status st = validate(problem);
+    if (st != GPP_OK) return st;
+    if (!out || !out->achtemp || !out->asxtemp)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "outputs achtemp/asxtemp are required");
+    const gpp_problem &h = *problem;
+    const size_t nb = (size_t)h.number_bands, nc = (size_t)h.ncouls, ng = (size_t)h.ngpown,
+                 nw = (size_t)h.nw;
+    const size_t wx_n = h.wx_stride ? nb * (size_t)h.wx_stride : nw;
+    struct Seg { const void *src; size_t bytes; size_t off; };
+    std::vector<Seg> in = {
+        {h.aqsmtemp, nb * nc * 16, 0}, {h.aqsntemp, nb * nc * 16, 0},
+        {h.I_eps_array, ng * nc * 16, 0}, {h.wtilde_array, ng * nc * 16, 0},
+        {h.vcoul, nc * 8, 0}, {h.inv_igp_index, ng * 4, 0},
+        {h.indinv, h.indinv ? nc * 4 : 0, 0}, {h.wx_array, wx_n * 8, 0}};
+    size_t off = 0;
+    for (auto &sg : in) { sg.off = off; off = align_up(off + sg.bytes); }
+    const size_t o_out = off;
+    off = align_up(off + 16 * (2 * nw + (out->acht_n1_loc ? nb : 0) + 1));
+    if (off > ctx->dev_bytes) {
+        if (ctx->dev) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(ctx->dev);
+            ctx->dev = nullptr;
+            ctx->dev_bytes = 0;
+        }
+        GPP_CUDA_TRY(cudaMalloc(&ctx->dev, off), "cudaMalloc(context buffers)");
+        ctx->dev_bytes = off;
+    }
+    char *d = static_cast<char *>(ctx->dev);
+    for (auto &sg : in)
+        if (sg.bytes)
+            GPP_CUDA_TRY(cudaMemcpyAsync(d + sg.off, sg.src, sg.bytes, cudaMemcpyHostToDevice, ctx->stream),
+                         "cudaMemcpyAsync(H2D)");
+    gpp_problem q = h;
+    q.aqsmtemp = reinterpret_cast<const gpp_complex *>(d + in[0].off);
+    q.aqsntemp = reinterpret_cast<const gpp_complex *>(d + in[1].off);
+    q.I_eps_array = reinterpret_cast<const gpp_complex *>(d + in[2].off);
+    q.wtilde_array = reinterpret_cast<const gpp_complex *>(d + in[3].off);
+    q.vcoul = reinterpret_cast<const double *>(d + in[4].off);
+    q.inv_igp_index = reinterpret_cast<const int *>(d + in[5].off);
+    q.indinv = h.indinv ? reinterpret_cast<const int *>(d + in[6].off) : nullptr;
+    q.wx_array = reinterpret_cast<const double *>(d + in[7].off);
+    gpp_complex *dout = reinterpret_cast<gpp_complex *>(d + o_out);
+    gpp_outputs o{};
+    o.achtemp = dout;
+    o.asxtemp = dout + nw;
+    o.achstemp = dout + 2 * nw;
+    o.acht_n1_loc = out->acht_n1_loc ? dout + 2 * nw + 1 : nullptr;
+    if (!out->achstemp) o.achstemp = nullptr;
+    st = gpp_sigma(&q, &o, reinterpret_cast<gpp_stream_t>(ctx->stream));
+    if (st != GPP_OK) return st;
+    const size_t out_bytes = 16 * (2 * nw + 1 + (out->acht_n1_loc ? nb : 0));
+    std::vector<gpp_complex> tmp(out_bytes / 16);
+    GPP_CUDA_TRY(cudaMemcpyAsync(tmp.data(), dout, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
+                 "cudaMemcpyAsync(D2H)");
+    st = gpp_wait(reinterpret_cast<gpp_stream_t>(ctx->stream), -1);
+    if (st != GPP_OK) return st;
+    memcpy(out->achtemp, tmp.data(), 16 * nw);
+    memcpy(out->asxtemp, tmp.data() + nw, 16 * nw);
+    if (out->achstemp) out->achstemp[0] = tmp[2 * nw];
+    if (out->acht_n1_loc) memcpy(out->acht_n1_loc, tmp.data() + 2 * nw + 1, 16 * nb);
+    return GPP_OK;
+}
+
+gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *outs, int nstates,
+                             gpp_stream_t stream) {
+    if (nstates < 0 || (nstates > 0 && (!problems || !outs)))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "bad batch");
+    for (int i = 0; i < nstates; ++i) {
+        gpp_status st = gpp_sigma(problems + i, outs + i, stream);
+        if (st != GPP_OK) return st;
+    }
+    return GPP_OK;
+}
+
+gpp_status gpp_enable_kernel_timing(int enable) {
+    t_timing = enable != 0;
+    if (t_timing && !t_ev0) {
+        GPP_CUDA_TRY(cudaEventCreate(&t_ev0), "cudaEventCreate");
+        GPP_CUDA_TRY(cudaEventCreate(&t_ev1), "cudaEventCreate");
+    }
+    t_timed = false;
+    return GPP_OK;
+}
+
+gpp_status gpp_last_kernel_ms(float *ms) {
+    if (!ms) return fail(GPP_ERR_INVALID_ARGUMENT, "ms is NULL");
+    if (!t_timed) return fail(GPP_ERR_NOT_READY, "no timed kernel yet (enable timing first)");
+    GPP_CUDA_TRY(cudaEventSynchronize(t_ev1), "cudaEventSynchronize");
+    GPP_CUDA_TRY(cudaEventElapsedTime(ms, t_ev0, t_ev1), "cudaEventElapsedTime");
+    return GPP_OK;
+}
+
+gpp_status gpp_probe_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
+    if (!fp64_tflops || !fp32_tflops) return fail(GPP_ERR_INVALID_ARGUMENT, "NULL output");
+    cudaError_t e = probe_fma_peaks(fp64_tflops, fp32_tflops);
+    if (e != cudaSuccess) return cuda_fail(e, "FMA probe");
+    return GPP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,490 @@
+// gpp_fp64.cu -- FP64 CUDA-core kernels of the GPP sigma reduction for
+// sm_103a, plus the deterministic fixed-order reduction and the static term.
+//
+// Algorithm (reference: noflagOCC_solver gppComplex_seq.cpp:131-150,
+// flagOCC_solver :107-128, ssxt_scht_solver :16-63, driver :335-383).
+// The unoccupied term is regrouped, exactly in real arithmetic, as
+//
+//   mygpvar1 aqsn (delw I_eps) = conj(aqsm[n1,igp]) * A * conj(wdiff) / |wdiff|^2
+//   A = aqsn[n1,ig] * (wtilde[igp,ig] * I_eps[igp,ig]),  wdiff = wx - wtilde
+//
+// so conj(aqsm) leaves the ig sum (applied once per (n1,igp) in the block
+// epilogue) and A is shared by all frequencies.  Per term the FP64 pipe then
+// does 9 instructions: wdiff.re (DADD), |wdiff|^2 (DFMA), the reciprocal (3
+// DFMA after a seed from the multi-function unit), A*conj(wdiff) (2 DFMA with
+// the iw-independent products hoisted) and the accumulation (2 DFMA).
+//
+// Work decomposition: a block owns RG local G' rows x RN bands x NWC
+// frequencies and all ncouls columns; its threads stride over ig, so every
+// global load is a coalesced 16-byte double2 (ld.global.nc) and each loaded
+// element is reused RN*NWC (rows) or RG*NWC (bands) times from registers.
+// On GB300 the FP64 pipe retires ~2 DFMA/clk/SM, so the kernel is bound by
+// FP64 issue, not by HBM (~16 B per (n1,igp,ig) triple against ~34 FP64
+// instructions).  Partial sums: per-thread registers -> warp shuffle tree ->
+// shared-memory tree across warps -> one complex per block and frequency in
+// the workspace -> gpp_reduce_kernel sums blocks in a fixed order.  No
+// floating-point atomics anywhere: results are bit-reproducible.
+#include <cstdio>
+
+#include "gpp_kernels.h"
+
+namespace gpp {
+
+namespace {
+
+// Block-wide reduction of K doubles per thread; result in out[K] (shared).
+template <int K, int THREADS>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double *red, double *out) {
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) red[warp * K + k] = s;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += THREADS) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < NWARP; ++w) s += red[w * K + k];
+        out[k] = s;
+    }
+    __syncthreads();
+}
+
+template <int RN, int RG, int NWC, int THREADS>
+__global__ void __launch_bounds__(THREADS)
+noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end) {
+    constexpr int K = RN * RG * NWC * 2;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+
+    const int row0 = blockIdx.x * RG;
+    const int band0 = band_begin + blockIdx.y * RN;
+    const int iw0 = blockIdx.z * NWC;
+    const int nc = p.nc;
+
+    const double2 *wrow[RG];
+    const double2 *erow[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const int r = min(row0 + g, p.ng - 1);
+        wrow[g] = p.wt + (size_t)r * nc;
+        erow[g] = p.ieps + (size_t)r * nc;
+    }
+    const double2 *nrow[RN];
+    double wx[RN][NWC];
+#pragma unroll
+    for (int n = 0; n < RN; ++n) {
+        const int b = min(band0 + n, band_end - 1);
+        nrow[n] = p.aqsn + (size_t)b * nc;
+#pragma unroll
+        for (int w = 0; w < NWC; ++w)
+            wx[n][w] = __ldg(p.wx + (size_t)b * p.wx_stride + min(iw0 + w, p.nw - 1));
+    }
+
+    double2 acc[RN][RG][NWC];
+#pragma unroll
+    for (int n = 0; n < RN; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) acc[n][g][w] = make_double2(0.0, 0.0);
+
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        double2 Q[RG];
+        double wtr[RG], wti[RG], wti2[RG];
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const double2 wt = __ldg(wrow[g] + ig);
+            const double2 ie = __ldg(erow[g] + ig);
+            Q[g] = cmul(wt, ie);
+            wtr[g] = wt.x;
+            wti[g] = wt.y;
+            wti2[g] = wt.y * wt.y;
+        }
+#pragma unroll
+        for (int n = 0; n < RN; ++n) {
+            const double2 a = __ldg(nrow[n] + ig);
+#pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const double2 A = cmul(a, Q[g]);
+                const double ayw = A.y * wti[g];
+                const double axw = A.x * wti[g];
+#pragma unroll
+                for (int w = 0; w < NWC; ++w) {
+                    const double wr = wx[n][w] - wtr[g];   // Re(wdiff); Im(wdiff) = -wti
+                    const double d = fma(wr, wr, wti2[g]); // |wdiff|^2
+                    const double r = rcp_fp64(d);
+                    const double tx = fma(A.x, wr, -ayw);  // A * conj(wdiff)
+                    const double ty = fma(A.y, wr, axw);
+                    acc[n][g][w].x = fma(r, tx, acc[n][g][w].x);
+                    acc[n][g][w].y = fma(r, ty, acc[n][g][w].y);
+                }
+            }
+        }
+    }
+
+    double v[K];
+#pragma unroll
+    for (int n = 0; n < RN; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const int k = ((n * RG + g) * NWC + w) * 2;
+                v[k] = acc[n][g][w].x;
+                v[k + 1] = acc[n][g][w].y;
+            }
+    block_reduce<K, THREADS>(v, red, S);
+
+    // Epilogue: weight each (n1, igp) sum by 0.5 vcoul[igp] conj(aqsm[n1,igp])
+    // (gppComplex_seq.cpp:146,374,379) and add the pairs in a fixed order.
+    const long long tile = (long long)blockIdx.y * gridDim.x + blockIdx.x + part.ach_tile0;
+    const int t = threadIdx.x;
+    if (t < NWC || (part.n1 && t >= 32 && t < 32 + RN)) {
+        const bool is_n1 = t >= 32;
+        double2 tot = make_double2(0.0, 0.0);
+        const int nlo = is_n1 ? t - 32 : 0, nhi = is_n1 ? t - 32 + 1 : RN;
+        const int w = is_n1 ? 2 - iw0 : t;
+        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
+            for (int n = nlo; n < nhi; ++n) {
+                const int b = band0 + n;
+                if (b >= band_end) continue;
+#pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    const int row = row0 + g;
+                    if (row >= p.ng) continue;
+                    const int igp = resolve_igp(p, row, part.err);
+                    if (igp < 0) continue;
+                    const double2 m = __ldg(p.aqsm + (size_t)b * nc + igp);
+                    const int k = ((n * RG + g) * NWC + w) * 2;
+                    const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
+                    tot = cadd(tot, cscale(cscale(s, 0.5), __ldg(p.vcoul + igp)));
+                }
+            }
+            if (!is_n1)
+                part.ach[(long long)(iw0 + w) * part.ach_seg + tile] = tot;
+            else if (band0 + nlo < band_end)
+                part.n1[(long long)(band0 + nlo) * part.n1_seg + blockIdx.x] = tot;
+        }
+    }
+}
+
+// One occupied-band term of ssxt_scht_solver (gppComplex_seq.cpp:16-63),
+// accumulated as aqsn*sch and aqsn*ssx (the conj(aqsm) factor of
+// matngmatmgp is applied in the epilogue).  cwr = 1/wx^2 for branch A.
+template <int SEM>
+__device__ __forceinline__ void flag_term(double wx, double cwr, double2 wt, double2 wt2,
+                                          double2 om2, double2 ie, double2 a, double2 &acc_s,
+                                          double2 &acc_x) {
+    const double2 wd = make_double2(wx - wt.x, -wt.y);
+    const double wdr = wd.x * wd.x + wd.y * wd.y;
+    const double rden = rcp_fp64(wdr);
+    const double2 delw = cscale(cmul_conj_b(wt, wd), rden);
+    const double delwr = delw.x * delw.x + delw.y * delw.y;
+    double2 sch = make_double2(0.0, 0.0), ssx = make_double2(0.0, 0.0);
+    if (wdr > kLimitTwo && delwr < kLimitOne) {
+        sch = cmul(delw, ie);
+        ssx = cscale(om2, cwr);
+    } else if (delwr > kTo1) {
+        const double2 cden = cscale(cmul(wt2, make_double2(0.5 + delw.x, delw.y)), 4.0);
+        const double r2 = rcp_fp64(cden.x * cden.x + cden.y * cden.y);
+        ssx = cmul(cmul_conj_b(make_double2(-om2.x, -om2.y), cden), cscale(delw, r2));
+    }
+    // |ssx| > sexcut |I_eps| compared on squares (sexcut^2 = 16 is exact).
+    if (SEM == kSemComplexSeq && wx < 0.0 &&
+        ssx.x * ssx.x + ssx.y * ssx.y > 16.0 * (ie.x * ie.x + ie.y * ie.y))
+        ssx = make_double2(0.0, 0.0);
+    acc_s = cadd(acc_s, cmul(a, sch));
+    acc_x = cadd(acc_x, cmul(a, ssx));
+}
+
+template <int RG, int NWC, int THREADS, int SEM>
+__global__ void __launch_bounds__(THREADS) flag_fp64_kernel(Problem p, Partials part) {
+    constexpr int K = RG * NWC * 4;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+
+    const int row0 = blockIdx.x * RG;
+    const int band = blockIdx.y;  // one occupied band per block row
+    const int iw0 = blockIdx.z * NWC;
+    const int nc = p.nc;
+
+    const double2 *wrow[RG];
+    const double2 *erow[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const int r = min(row0 + g, p.ng - 1);
+        wrow[g] = p.wt + (size_t)r * nc;
+        erow[g] = p.ieps + (size_t)r * nc;
+    }
+    const double2 *nrow = p.aqsn + (size_t)band * nc;
+    double wx[NWC], cwr[NWC];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w) {
+        wx[w] = __ldg(p.wx + (size_t)band * p.wx_stride + min(iw0 + w, p.nw - 1));
+        const double c = wx[w] * wx[w];
+        cwr[w] = c / (c * c);  // wx^2 / pow(wx^2, 2), once per (band, iw)
+    }
+
+    double2 acc_s[RG][NWC], acc_x[RG][NWC];
+#pragma unroll
+    for (int g = 0; g < RG; ++g)
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            acc_s[g][w] = make_double2(0.0, 0.0);
+            acc_x[g][w] = make_double2(0.0, 0.0);
+        }
+
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        const double2 a = __ldg(nrow + ig);
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const double2 wt = __ldg(wrow[g] + ig);
+            const double2 ie = __ldg(erow[g] + ig);
+            const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
+            const double2 om2 = cmul(wt2, ie);
+#pragma unroll
+            for (int w = 0; w < NWC; ++w)
+                flag_term<SEM>(wx[w], cwr[w], wt, wt2, om2, ie, a, acc_s[g][w], acc_x[g][w]);
+        }
+    }
+
+    double v[K];
+#pragma unroll
+    for (int g = 0; g < RG; ++g)
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            const int k = (g * NWC + w) * 4;
+            v[k] = acc_s[g][w].x;
+            v[k + 1] = acc_s[g][w].y;
+            v[k + 2] = acc_x[g][w].x;
+            v[k + 3] = acc_x[g][w].y;
+        }
+    block_reduce<K, THREADS>(v, red, S);
+
+    const long long tile = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+    const int t = threadIdx.x;
+    // t < NWC: achtemp partial; NWC <= t < 2 NWC: asxtemp partial; t == 64: n1 column.
+    const bool do_ach = t < NWC, do_asx = t >= NWC && t < 2 * NWC, do_n1 = part.n1 && t == 64;
+    if (do_ach || do_asx || do_n1) {
+        const int w = do_ach ? t : (do_asx ? t - NWC : 2 - iw0);
+        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
+            double2 tot = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int row = row0 + g;
+                if (row >= p.ng) continue;
+                const int igp = resolve_igp(p, row, part.err);
+                if (igp < 0) continue;
+                const double2 m = __ldg(p.aqsm + (size_t)band * nc + igp);
+                const int k = (g * NWC + w) * 4 + (do_asx ? 2 : 0);
+                const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
+                const double v_igp = __ldg(p.vcoul + igp);
+                tot = cadd(tot, do_asx ? cscale(s, p.occ * v_igp) : cscale(cscale(s, 0.5), v_igp));
+            }
+            if (do_ach)
+                part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + tile] = tot;
+            else if (do_asx)
+                part.asx[(long long)(iw0 + w) * part.asx_seg + tile] = tot;
+            else
+                part.n1[(long long)band * part.n1_seg + blockIdx.x] = tot;
+        }
+    }
+}
+
+// Static term of reduce_achstemp (gppComplex_seq.cpp:66-101): one thread per
+// (n1, my_igp) pair; each block leaves one partial.
+__global__ void __launch_bounds__(256) achstemp_kernel(Problem p, double2 *partials, int *err) {
+    __shared__ double red[8 * 2];
+    __shared__ double S[2];
+    const long long npairs = (long long)p.nb * p.ng;
+    const long long pr = (long long)blockIdx.x * 256 + threadIdx.x;
+    double v[2] = {0.0, 0.0};
+    if (pr < npairs) {
+        const int n1 = (int)(pr / p.ng), my_igp = (int)(pr % p.ng);
+        const int igp = resolve_igp(p, my_igp, err);
+        if (igp >= 0) {
+            const double2 m = __ldg(p.aqsm + (size_t)n1 * p.nc + igp);
+            const double2 an = __ldg(p.aqsn + (size_t)n1 * p.nc + igp);
+            const double2 ie = __ldg(p.ieps + (size_t)my_igp * p.nc + igp);
+            const double2 schs = make_double2(-ie.x, -ie.y);
+            const double2 matng = cmul(an, make_double2(m.x, -m.y));
+            if (sqrt(schs.x * schs.x + schs.y * schs.y) > kTo1) {
+                const double2 c = cscale(cmul(matng, schs), __ldg(p.vcoul + igp) * 0.5);
+                v[0] = c.x;
+                v[1] = c.y;
+            }
+        }
+    }
+    block_reduce<2, 256>(v, red, S);
+    if (threadIdx.x == 0) partials[blockIdx.x] = make_double2(S[0], S[1]);
+}
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS)
+reduce_kernel(const double2 *src, long long stride, int len, ReduceOut out) {
+    __shared__ double red[(THREADS / 32) * 2];
+    __shared__ double S[2];
+    const double2 *seg = src + (long long)blockIdx.x * stride;
+    double v[2] = {0.0, 0.0};
+    for (int t = threadIdx.x; t < len; t += THREADS) {
+        const double2 x = seg[t];
+        v[0] += x.x;
+        v[1] += x.y;
+    }
+    block_reduce<2, THREADS>(v, red, S);
+    if (threadIdx.x == 0) {
+        const int s = blockIdx.x;
+        if (out.c) {
+            double2 r = make_double2(S[0], S[1]);
+            if (out.accumulate) r = cadd(out.c[s], r);
+            out.c[s] = r;
+        }
+        if (out.re) out.re[s] += S[0];
+        if (out.im) out.im[s] += S[1];
+    }
+}
+
+template <int RN, int RG, int NWC, int THREADS>
+cudaError_t launch_noflag_t(const Problem &p, const Partials &part, int b0, int b1,
+                            cudaStream_t s) {
+    dim3 grid(ceil_div(p.ng, RG), ceil_div(b1 - b0, RN), ceil_div(p.nw, NWC));
+    noflag_fp64_kernel<RN, RG, NWC, THREADS><<<grid, THREADS, 0, s>>>(p, part, b0, b1);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <int RG, int NWC, int THREADS>
+cudaError_t launch_flag_t(const Problem &p, const Partials &part, cudaStream_t s) {
+    dim3 grid(ceil_div(p.ng, RG), p.nv, ceil_div(p.nw, NWC));
+    if (p.semantics == kSemKerSeq)
+        flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(p, part);
+    else
+        flag_fp64_kernel<RG, NWC, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(p, part);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Frequencies per block: a whole small frequency grid stays in registers; a
+// large grid (e.g. 32 frequencies) is split into chunks of 8.
+static int nwc_for(int nw) { return nw <= 4 ? nw : 8; }
+
+TileShape fp64_noflag_shape(const Problem &p) {
+    const int nwc = nwc_for(p.nw);
+    return nwc <= 4 ? TileShape{4, 2, nwc, 128} : TileShape{2, 2, nwc, 128};
+}
+
+TileShape flag_shape(const Problem &p) { return TileShape{1, 2, nwc_for(p.nw), 128}; }
+
+cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int b0, int b1,
+                               cudaStream_t s) {
+    if (b1 <= b0 || p.ng == 0) return cudaSuccess;
+    switch (nwc_for(p.nw)) {
+        case 1: return launch_noflag_t<4, 2, 1, 128>(p, part, b0, b1, s);
+        case 2: return launch_noflag_t<4, 2, 2, 128>(p, part, b0, b1, s);
+        case 3: return launch_noflag_t<4, 2, 3, 128>(p, part, b0, b1, s);
+        case 4: return launch_noflag_t<4, 2, 4, 128>(p, part, b0, b1, s);
+        default: return launch_noflag_t<2, 2, 8, 128>(p, part, b0, b1, s);
+    }
+}
+
+cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s) {
+    if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
+    switch (nwc_for(p.nw)) {
+        case 1: return launch_flag_t<2, 1, 128>(p, part, s);
+        case 2: return launch_flag_t<2, 2, 128>(p, part, s);
+        case 3: return launch_flag_t<2, 3, 128>(p, part, s);
+        case 4: return launch_flag_t<2, 4, 128>(p, part, s);
+        default: return launch_flag_t<2, 8, 128>(p, part, s);
+    }
+}
+
+int achstemp_blocks(const Problem &p) { return ceil_div((long long)p.nb * p.ng, 256); }
+
+cudaError_t launch_achstemp(const Problem &p, double2 *partials, int *err, cudaStream_t s) {
+    const int blocks = achstemp_blocks(p);
+    if (blocks == 0) return cudaSuccess;
+    achstemp_kernel<<<blocks, 256, 0, s>>>(p, partials, err);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const double2 *src, long long stride, int len, int nseg, ReduceOut out,
+                          cudaStream_t s) {
+    if (nseg <= 0) return cudaSuccess;
+    reduce_kernel<512><<<nseg, 512, 0, s>>>(src, stride, len, out);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FMA throughput probe: independent FMA chains, enough warps to fill the SMs.
+namespace {
+template <typename T, int CHAINS>
+__global__ void __launch_bounds__(256) fma_probe_kernel(const T *in, T *out, int iters) {
+    T a[CHAINS];
+    const T b = in[0], c = in[1];
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) a[k] = in[2 + k] + (T)threadIdx.x;
+    for (int i = 0; i < iters; ++i)
+#pragma unroll
+        for (int k = 0; k < CHAINS; ++k) a[k] = fma(a[k], b, c);
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < CHAINS; ++k) s += a[k];
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+cudaError_t time_probe(int blocks, int iters, double *tflops) {
+    constexpr int CHAINS = 8;
+    T *in = nullptr, *out = nullptr;
+    cudaError_t e = cudaMalloc(&in, 16 * sizeof(T));
+    if (e != cudaSuccess) return e;
+    e = cudaMalloc(&out, (size_t)blocks * 256 * sizeof(T));
+    if (e != cudaSuccess) { cudaFree(in); return e; }
+    T h[16];
+    for (int i = 0; i < 16; ++i) h[i] = (T)(1.0 + 1e-7 * i);
+    h[0] = (T)0.999999;
+    h[1] = (T)1e-6;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.f;
+    e = cudaMemcpy(in, h, sizeof(h), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) {
+        fma_probe_kernel<T, CHAINS><<<blocks, 256>>>(in, out, iters / 8);  // warm-up
+        count_launch();
+        cudaEventRecord(e0);
+        fma_probe_kernel<T, CHAINS><<<blocks, 256>>>(in, out, iters);
+        count_launch();
+        cudaEventRecord(e1);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && ms > 0.f)
+            *tflops = 2.0 * blocks * 256.0 * CHAINS * (double)iters / (ms * 1e-3) * 1e-12;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(in);
+    cudaFree(out);
+    return e;
+}
+}  // namespace
+
+cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    const int blocks = sms * 8;
+    e = time_probe<double>(blocks, 4096, fp64_tflops);
+    if (e == cudaSuccess) e = time_probe<float>(blocks, 65536, fp32_tflops);
+    return e;
+}
+
+}  // namespace gpp

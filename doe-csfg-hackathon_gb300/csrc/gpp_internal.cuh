@@ -1,0 +1,116 @@
+// gpp_internal.cuh -- shared device-side definitions of the GB300 GPP sigma
+// kernels (FP64, mixed precision, batched) and the host dispatcher.
+//
+// Data layout in HBM (caller-owned, unchanged from the reference,
+// gppKerSeq.cpp:194-197): complex128 arrays interleaved {re,im}, row-major;
+// aqsntemp/aqsmtemp [number_bands][ncouls], I_eps/wtilde [ngpown][ncouls].
+// Library scratch (per-device workspace): per-block partial sums (complex128)
+// reduced in a fixed order by gpp_reduce_kernel, and for the mixed path the
+// float-float split copies of the inputs made by the prep kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpp {
+
+// Constants of ssxt_scht_solver (gppComplex_seq.cpp:20-23) and of the main
+// drivers (gppComplex_seq.cpp:241-247).
+constexpr double kTo1 = 1e-6;
+constexpr double kSexcut = 4.0;
+constexpr double kLimitOne = 1.0 / (kTo1 * 4.0);
+constexpr double kLimitTwo = 0.25;  // pow(0.5, 2)
+
+enum : int { kSemComplexSeq = 0, kSemKerSeq = 1 };
+
+// Device-side fault bits (workspace word, read by gpp_wait).
+enum : int { kErrBadIgp = 1, kErrBadIndinv = 2 };
+
+// Everything a sigma kernel needs about one problem (one quasiparticle
+// state).  Passed by value as a kernel parameter or read from a table by the
+// batched kernel.
+struct Problem {
+    const double2 *aqsm;   // [nb][nc]
+    const double2 *aqsn;   // [nb][nc]
+    const double2 *ieps;   // [ng][nc]
+    const double2 *wt;     // [ng][nc]
+    const double *vcoul;   // [nc]
+    const int *inv_igp;    // [ng]
+    const int *indinv;     // [nc] or null
+    const double *wx;      // wx(n1, iw) = wx[n1 * wx_stride + iw]
+    int wx_stride;
+    int nb, nv, nc, ng, nw;
+    double occ;
+    int semantics;
+};
+
+// Where one launch writes its per-block partial sums.  Segment layouts:
+//   ach[iw * ach_seg + tile]   (ach_seg = tiles of all launches of the call)
+//   asx[iw * asx_seg + tile]   (occupied-band launches only)
+//   n1[band * n1_seg + row_tile] (acht_n1_loc, only when nw >= 3)
+struct Partials {
+    double2 *ach;
+    long long ach_seg;
+    int ach_tile0;   // first tile index of this launch inside the ach segment
+    double2 *asx;
+    long long asx_seg;
+    double2 *n1;     // may be null
+    int n1_seg;
+    int *err;        // device fault word
+};
+
+// Resolve the G' column index of local row my_igp exactly like the reference
+// (gppComplex_seq.cpp:342-344: values >= ncouls clamp to ncouls-1), then the
+// optional indinv remap.  Returns -1 (and raises a fault bit) for indices the
+// reference would read out of bounds.
+__device__ __forceinline__ int resolve_igp(const Problem &p, int my_igp, int *err) {
+    int igp = __ldg(p.inv_igp + my_igp);
+    if (igp >= p.nc) igp = p.nc - 1;
+    if (igp < 0) {
+        atomicOr(err, kErrBadIgp);
+        return -1;
+    }
+    if (p.indinv) {
+        igp = __ldg(p.indinv + igp);
+        if (igp < 0 || igp >= p.nc) {
+            atomicOr(err, kErrBadIndinv);
+            return -1;
+        }
+    }
+    return igp;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmul_conj_b(double2 a, double2 b) {  // a * conj(b)
+    return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+    return make_double2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) {
+    return make_double2(a.x * s, a.y * s);
+}
+
+// FP64 reciprocal: hardware seed (rcp.approx.ftz.f64, issued to the
+// multi-function unit, not the FP64 pipe) refined by one cubic Newton-Raphson
+// step r = r0 (1 + e + e^2), e = 1 - d r0 (the classical Newton iteration for
+// 1/d with the second-order term kept).  Three FP64 FMAs instead of the ~5
+// FMA-equivalents of an IEEE division; the error is within about one ulp.
+__device__ __forceinline__ double rcp_fp64(double d) {
+    double r0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(d));
+    double e = fma(-d, r0, 1.0);
+    double t = fma(e, e, e);
+    return fma(r0, t, r0);
+}
+
+// Warp-level sum of a double with a fixed shuffle tree (deterministic).
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+}  // namespace gpp

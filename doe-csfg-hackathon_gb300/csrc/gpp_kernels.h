@@ -1,0 +1,56 @@
+// gpp_kernels.h -- host-side launchers of the GPP sigma kernels (internal to
+// libgpp_gb300.so; the public C ABI is include/gpp_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gpp_internal.cuh"
+
+namespace gpp {
+
+// Tile geometry of one family of sigma kernels.  Blocks cover RG local G'
+// rows x RN bands x NWC frequencies; the block's threads stride over ig.
+struct TileShape {
+    int rn, rg, nwc, threads;
+};
+
+// Shapes the launchers will use for this problem (also needed to size the
+// partial-sum workspace before launching).
+TileShape fp64_noflag_shape(const Problem &p);
+TileShape flag_shape(const Problem &p);
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Unoccupied bands [band_begin, band_end), FP64.  Writes one ach partial per
+// (row tile, band tile) block and, when part.n1 is set, per-band partials.
+cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int band_begin,
+                               int band_end, cudaStream_t s);
+// Occupied bands [0, nvband): full ssxt_scht_solver branch logic in FP64.
+cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s);
+// Static term (reduce_achstemp) over all bands: one partial per block.
+int achstemp_blocks(const Problem &p);
+cudaError_t launch_achstemp(const Problem &p, double2 *partials, int *err, cudaStream_t s);
+
+// Fixed-order sum of segments: dst[s] (=|+=) sum_{t<len} src[s*stride + t].
+struct ReduceOut {
+    double2 *c;      // complex destination (or null)
+    double *re;      // split destination, always accumulated (or null)
+    double *im;
+    int accumulate;  // for c: 1 adds into c[s], 0 overwrites
+};
+cudaError_t launch_reduce(const double2 *src, long long stride, int len, int nseg, ReduceOut out,
+                          cudaStream_t s);
+
+// FMA throughput probe (see gpp_probe_fma_peaks).
+cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+
+// Mixed precision path (gpp_mixed.cu).
+size_t mixed_split_bytes(const Problem &p);
+TileShape mixed_noflag_shape(const Problem &p);
+cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws,
+                                int band_begin, int band_end, cudaStream_t s);
+
+// Per-thread launch counter (gpp_launch_count).
+void count_launch(int n = 1);
+
+}  // namespace gpp

@@ -1,0 +1,204 @@
+/*
+ * gpp_gb300.h -- C ABI of the GB300-native GPP sigma library (libgpp_gb300.so).
+ *
+ * The General Plasmon Pole (GPP) sigma reduction of the DOE-CSFG-hackathon
+ * mini-app (BerkeleyGW kernel): for bands n1, local G' rows my_igp, G columns
+ * ig and frequencies iw,
+ *
+ *   achtemp[iw] += sum_{n1,my_igp} vcoul[igp] * 0.5 * scht(n1,my_igp,iw)
+ *   asxtemp[iw] += sum_{n1<nvband,my_igp} occ * vcoul[igp] * ssxt(n1,my_igp,iw)
+ *
+ * with scht/ssxt the ig sums of noflagOCC_solver / flagOCC_solver
+ * (gppComplex_seq.cpp:107-150) and igp = min(inv_igp_index[my_igp], ncouls-1).
+ *
+ * Conventions shared by every entry point:
+ *  - Complex arrays are interleaved {re, im} doubles (16 bytes), row-major:
+ *    aqsmtemp/aqsntemp [number_bands][ncouls], I_eps_array/wtilde_array
+ *    [ngpown][ncouls] (gppKerSeq.cpp:194-197).  gpp_complex has the layout of
+ *    the reference's GPPComplex (GPPComplex.h:68, a double2) and of
+ *    std::complex<double>.
+ *  - Unless stated otherwise, pointers are DEVICE pointers owned by the
+ *    caller (as in gppCudaVer.cpp:306-318) and launches are asynchronous on
+ *    the given stream (NULL = legacy default stream, as the reference uses).
+ *  - Every entry point returns a gpp_status and never exits the process.
+ *  - Results are deterministic: no floating-point atomics; every sum runs in
+ *    a fixed order, so repeated calls give bit-identical outputs.
+ */
+#ifndef GPP_GB300_H
+#define GPP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPP_GB300_VERSION_MAJOR 1
+#define GPP_GB300_VERSION_MINOR 0
+
+typedef struct gpp_complex { double re, im; } gpp_complex;
+
+/* cudaStream_t without pulling in CUDA headers (same underlying type). */
+typedef struct CUstream_st *gpp_stream_t;
+
+typedef enum gpp_status {
+    GPP_OK = 0,
+    GPP_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, overflow, bad enum */
+    GPP_ERR_CUDA = 2,             /* a CUDA runtime call failed (gpp_last_error_message) */
+    GPP_ERR_OUT_OF_MEMORY = 3,    /* workspace or staging allocation failed */
+    GPP_ERR_UNSUPPORTED = 4,      /* option not available for these sizes */
+    GPP_ERR_BAD_INDEX = 5,        /* device saw inv_igp_index < 0 or indinv out of range */
+    GPP_ERR_NOT_READY = 6         /* gpp_wait timed out; the work is still running */
+} gpp_status;
+
+typedef enum gpp_precision {
+    GPP_PRECISION_FP64 = 0,  /* FP64 CUDA-core kernel (<= 1e-12 rel vs the reference) */
+    GPP_PRECISION_MIXED = 1  /* float-float bulk, FP64 near the plasmon pole (<= 1e-8 rel) */
+} gpp_precision;
+
+typedef enum gpp_semantics {
+    /* gppComplex_seq.cpp / GPPComplex.cu: ssx is zeroed when
+     * |ssx| > 4|I_eps| and wx < 0 (gppComplex_seq.cpp:58-59). Default. */
+    GPP_SEM_COMPLEX_SEQ = 0,
+    /* gppKerSeq.cpp: the cutoff condition abs(wx) < 0 never holds (:60). */
+    GPP_SEM_KERSEQ = 1
+} gpp_semantics;
+
+/* ------------------------------------------------------------------------
+ * Drop-in entry points with the reference's argument lists.
+ * They take the stream set by gpp_set_stream() (default: legacy stream),
+ * use the band-independent wx_array[nend-nstart] of the reference, the
+ * GPP_SEM_COMPLEX_SEQ semantics of GPPComplex.cu, FP64 arithmetic, and ADD
+ * into the caller's output arrays (the reference accumulates with atomics
+ * into caller-zeroed arrays, gppCudaVer.cpp:360-361,376-377).
+ * ------------------------------------------------------------------------ */
+
+/* Replaces gppKernelGPU, declared at GPPComplex.h:304 and never defined in
+ * the reference.  No nvband argument: every band takes the unoccupied
+ * (noflagOCC) path.  indinv may be NULL; when given (ncouls entries) the
+ * clamped igp is remapped as igp = indinv[igp] (identity in every reference
+ * workload).  Frequencies iw = nstart .. nend-1 use wx_array[iw - nstart];
+ * achtemp_re/im are indexed by iw - nstart. */
+gpp_status gpp_kernel_gpu(const gpp_complex *wtilde_array, const gpp_complex *aqsntemp,
+                          const gpp_complex *aqsmtemp, const gpp_complex *I_eps_array,
+                          int ncouls, int ngpown, int number_bands, const double *wx_array,
+                          double *achtemp_re, double *achtemp_im, const double *vcoul,
+                          int nstart, int nend, const int *indinv, const int *inv_igp_index);
+
+/* Replaces d_till_nvband (GPPComplex.cu:406, declared GPPComplex.h:306):
+ * occupied bands n1 < nvband, 3 frequencies.  Adds into achtemp_re/im[3],
+ * asxtemp[3] and acht_n1_loc[n1] (iw = 2 column).  Deterministic where the
+ * reference's asxtemp / acht_n1_loc updates race (GPPComplex.cu:239,247). */
+gpp_status gpp_till_nvband(int nvband, int ngpown, int ncouls, const int *inv_igp_index,
+                           const double *wx_array, const gpp_complex *wtilde_array,
+                           const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                           const gpp_complex *I_eps_array, gpp_complex *asxtemp,
+                           const double *vcoul, gpp_complex *acht_n1_loc, double *achtemp_re,
+                           double *achtemp_im, double occ);
+
+/* Replaces d_noFlagOCCSolver (GPPComplex.cu:422, declared GPPComplex.h:310):
+ * unoccupied bands nvband <= n1 < number_bands, 3 frequencies.  Adds into
+ * achtemp_re/im[3] and acht_n1_loc[n1]. */
+gpp_status gpp_noflag_occ_solver(int number_bands, int nvband, int ngpown, int ncouls,
+                                 const int *inv_igp_index, const double *wx_array,
+                                 const gpp_complex *wtilde_array, const gpp_complex *aqsmtemp,
+                                 const gpp_complex *aqsntemp, const gpp_complex *I_eps_array,
+                                 const double *vcoul, double *achtemp_re, double *achtemp_im,
+                                 gpp_complex *acht_n1_loc);
+
+/* Replaces the host-side reduce_achstemp loop of gppCudaVer.cpp:385-386
+ * (gppKerSeq.cpp:67-100; d_reduce_achstemp is declared at GPPComplex.h:308
+ * but never defined): the static COHSEX term over all bands, ADDED into
+ * achstemp[0]. */
+gpp_status gpp_reduce_achstemp(int number_bands, const int *inv_igp_index, int ncouls,
+                               const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                               const gpp_complex *I_eps_array, gpp_complex *achstemp,
+                               int ngpown, const double *vcoul);
+
+/* Stream used by the drop-in entry points above (per host thread). */
+gpp_status gpp_set_stream(gpp_stream_t stream);
+gpp_stream_t gpp_get_stream(void);
+
+/* ------------------------------------------------------------------------
+ * Full problem API: occupied and unoccupied bands in one call, per-band
+ * frequencies, asxtemp, precision and semantics selection.
+ * ------------------------------------------------------------------------ */
+
+typedef struct gpp_problem {
+    int number_bands, nvband, ncouls, ngpown, nw;
+    const gpp_complex *aqsmtemp;     /* [number_bands][ncouls] */
+    const gpp_complex *aqsntemp;     /* [number_bands][ncouls] */
+    const gpp_complex *I_eps_array;  /* [ngpown][ncouls] */
+    const gpp_complex *wtilde_array; /* [ngpown][ncouls] */
+    const double *vcoul;             /* [ncouls] */
+    const int *inv_igp_index;        /* [ngpown]; values >= ncouls clamp to ncouls-1 */
+    const int *indinv;               /* [ncouls] or NULL (see gpp_kernel_gpu) */
+    const double *wx_array;          /* wx(n1,iw) = wx_array[n1*wx_stride + iw] */
+    int wx_stride;                   /* 0: one [nw] row for all bands; >= nw: per band */
+    double occ;                      /* occupation factor of asxtemp (reference: 1.0) */
+    int semantics;                   /* gpp_semantics */
+    int precision;                   /* gpp_precision */
+} gpp_problem;
+
+typedef struct gpp_outputs {
+    gpp_complex *achtemp;     /* [nw], OVERWRITTEN (required) */
+    gpp_complex *asxtemp;     /* [nw], OVERWRITTEN (required) */
+    gpp_complex *acht_n1_loc; /* [number_bands] or NULL; needs nw >= 3 (iw = 2 column) */
+    gpp_complex *achstemp;    /* [1] or NULL: static term of reduce_achstemp */
+} gpp_outputs;
+
+/* Device pointers in and out, asynchronous on `stream`.  Scratch memory comes
+ * from a per-device workspace that the library grows on demand (the first
+ * call at a larger size allocates; later calls do not). */
+gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_stream_t stream);
+
+/* Waits for `stream` (at most timeout_ms; < 0 waits forever) and reports
+ * device-side faults of earlier gpp_sigma calls on this device: returns
+ * GPP_ERR_BAD_INDEX once if a kernel saw an invalid index (and clears the
+ * flag), GPP_ERR_NOT_READY on timeout. */
+gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms);
+
+/* Host-memory convenience path (end-to-end): every array pointer in
+ * `problem` is a HOST pointer (pinned memory gives full copy speed), as are
+ * the outputs.  The call copies inputs to device buffers owned by `ctx`, runs
+ * gpp_sigma on the context's stream, copies results back and returns when
+ * they are on the host. */
+typedef struct gpp_context gpp_context;
+gpp_status gpp_context_create(gpp_context **ctx);
+gpp_status gpp_context_destroy(gpp_context *ctx);
+gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gpp_outputs *out);
+
+/* ------------------------------------------------------------------------
+ * Batched states: many independent quasiparticle states (uneven sizes) in
+ * one persistent launch over a work queue of (state, band tile, row tile).
+ * ------------------------------------------------------------------------ */
+gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *outs, int nstates,
+                             gpp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Introspection and measurement support.
+ * ------------------------------------------------------------------------ */
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char *gpp_last_error_message(void);
+
+/* Number of kernel launches issued by this library on this host thread
+ * since the last reset (for launch accounting in benchmarks). */
+unsigned long long gpp_launch_count(void);
+void gpp_reset_launch_count(void);
+
+/* Kernel timing hook: when enabled, gpp_sigma records CUDA events around
+ * its dominant kernel on the launching stream; gpp_last_kernel_ms returns
+ * the elapsed milliseconds of the most recent call (synchronises on the
+ * end event). */
+gpp_status gpp_enable_kernel_timing(int enable);
+gpp_status gpp_last_kernel_ms(float *ms);
+
+/* Measured FP64 / FP32 fused multiply-add peaks of the current device in
+ * TFLOP/s (FMA = 2 flops), from a short dependent-chain-free probe kernel. */
+gpp_status gpp_probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPP_GB300_H */

@@ -1,0 +1,94 @@
+"""Build recipe for the oracle -- TEST INFRASTRUCTURE ONLY.
+
+Two products:
+
+* ``oracle/_build/libgpp_oracle.so`` -- the C restatement (gpp_oracle.c),
+  compiled with ``-ffp-contract=off`` so x86 and Arm hosts give the same bits.
+  Built wherever the tests or the benchmark's CPU leg run.
+* ``oracle/_ref/`` -- the reference's own sequential code, compiled from its
+  sources where they lie (only where the reference checkout is present; it is
+  never copied into this repository):
+    - ``libref_complex_seq.so``: gppComplex_seq.cpp + ref_harness.cpp
+    - ``libref_kerseq.so``:      gppKerSeq.cpp      + ref_harness.cpp
+    - ``gppKerSeq.ex``, ``gppComplex_seq.ex``, ``gppOpenMP3.ex``: the
+      unmodified reference executables (README known-answer runs, CPU timing).
+  The reference's main() is renamed with -Dmain=... in the library builds.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+DEFAULT_REF_DIR = "/root/reference"
+
+ORACLE_SO = os.path.join(BUILD, "libgpp_oracle.so")
+
+
+def _run(cmd: list[str]) -> None:
+    subprocess.run(cmd, check=True)
+
+
+def _stale(target: str, sources: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(s) > t for s in sources)
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the C restatement into oracle/_build/libgpp_oracle.so."""
+    os.makedirs(BUILD, exist_ok=True)
+    srcs = [os.path.join(HERE, "gpp_oracle.c"), os.path.join(HERE, "gpp_oracle.h")]
+    if force or _stale(ORACLE_SO, srcs):
+        base = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
+                os.path.join(HERE, "gpp_oracle.c"), "-o", ORACLE_SO + ".tmp", "-lm"]
+        try:
+            _run(base[:1] + ["-fopenmp"] + base[1:])
+        except subprocess.CalledProcessError:
+            _run(base)  # no OpenMP runtime on this host: single-threaded oracle
+        os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool:
+    """Compile the reference's own CPU code into oracle/_ref/ (returns False
+    when the reference sources are not present on this machine)."""
+    if not os.path.isfile(os.path.join(ref_dir, "gppComplex_seq.cpp")):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    harness = os.path.join(HERE, "ref_harness.cpp")
+    common = ["g++", "-O3", "-ffp-contract=off", "-fPIC", "-w", "-I", ref_dir, "-I", HERE]
+    libs = [("libref_complex_seq.so", "gppComplex_seq.cpp", "REF_COMPLEX_SEQ"),
+            ("libref_kerseq.so", "gppKerSeq.cpp", "REF_KERSEQ")]
+    for out, src, macro in libs:
+        target = os.path.join(REF_OUT, out)
+        srcp = os.path.join(ref_dir, src)
+        if force or _stale(target, [srcp, harness]):
+            _run(common + ["-shared", "-D" + macro, "-Dmain=gpp_reference_unused_main",
+                           srcp, harness, "-o", target])
+    exes = [("gppKerSeq.ex", "gppKerSeq.cpp", []),
+            ("gppComplex_seq.ex", "gppComplex_seq.cpp", []),
+            ("gppOpenMP3.ex", "gppOpenMP3.cpp", ["-fopenmp"])]
+    for out, src, extra in exes:
+        target = os.path.join(REF_OUT, out)
+        srcp = os.path.join(ref_dir, src)
+        if force or _stale(target, [srcp]):
+            _run(["g++", "-O3", "-w", "-I", ref_dir] + extra + [srcp, "-o", target])
+    return True
+
+
+def main() -> int:
+    build_oracle(force="--force" in sys.argv)
+    ok = build_reference(force="--force" in sys.argv)
+    print("oracle:", ORACLE_SO)
+    print("reference:", REF_OUT if ok else "not present on this machine")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

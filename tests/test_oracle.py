@@ -1,0 +1,88 @@
+"""The oracle (C restatement of the reference's CPU path) against the
+reference's published known answers and its own outputs (golden fixtures)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import case_inputs, load_golden, unhex
+import oracle_py
+from gppsigma import workload as W
+
+CASES = load_golden()
+
+
+def fmt(z):
+    return "(%.15g,%.15g)" % (z.real, z.imag)
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["kind"] == "ramp"], ids=lambda c: c["name"])
+@pytest.mark.parametrize("semantics", ["kerseq", "complex_seq"])
+def test_readme_known_answers(case, semantics):
+    """README.md:26-41: achtemp printed with 15 significant digits."""
+    r = oracle_py.run(case_inputs(case), semantics, nthreads=4)
+    assert [fmt(z) for z in r["achtemp"]] == case["readme_achtemp"]
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+def test_oracle_bit_exact_vs_reference_outputs(case):
+    inp = case_inputs(case)
+    assert inp.digest() == case["digest"], "input generator drifted"
+    r = oracle_py.run(inp, case["semantics"], nthreads=4)
+    for key in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
+        want = unhex(case[key])
+        if want is None:
+            continue
+        np.testing.assert_array_equal(r[key], want, err_msg=key)
+
+
+def test_thread_count_does_not_change_bits():
+    inp = W.make_inputs(W.Shape(12, 3, 900, 17, 3), 21)
+    a = oracle_py.run(inp, nthreads=1)
+    b = oracle_py.run(inp, nthreads=6)
+    for k in a:
+        if a[k] is not None:
+            np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_openmp_loop_shape_agrees():
+    inp = W.make_inputs(W.Shape(12, 3, 900, 17, 3), 22)
+    a = oracle_py.run(inp, nthreads=1)
+    b = oracle_py.run(inp, impl="oracle_omp", nthreads=4)
+    for k in ("achtemp", "asxtemp"):
+        np.testing.assert_allclose(b[k], a[k], rtol=1e-12, atol=0)
+
+
+def test_band_subsets_add_up():
+    inp = W.make_inputs(W.Shape(10, 3, 600, 9, 3), 23)
+    full = oracle_py.run(inp)
+    parts = [oracle_py.run(inp, band_begin=a, band_end=b) for a, b in ((0, 4), (4, 10))]
+    np.testing.assert_allclose(parts[0]["achtemp"] + parts[1]["achtemp"], full["achtemp"], rtol=1e-12)
+    np.testing.assert_allclose(parts[0]["asxtemp"] + parts[1]["asxtemp"], full["asxtemp"], rtol=1e-12)
+
+
+def test_negative_index_rejected():
+    inp = W.make_inputs(W.Shape(4, 1, 64, 4, 3), 24)
+    inp.inv_igp_index[1] = -1
+    with pytest.raises(ValueError):
+        oracle_py.run(inp)
+
+
+def test_planted_mistake_is_caught():
+    """A 1e-10 relative change of a single wtilde entry (one of 10k) must move
+    the outputs off the reference fixture: the bit-exact comparison is sensitive."""
+    case = next(c for c in CASES if c["name"] == "ragged_complex_seq")
+    inp = case_inputs(case)
+    inp.wtilde_array[3, 5] *= 1.0 + 1e-10
+    r = oracle_py.run(inp, case["semantics"])
+    assert not np.array_equal(r["achtemp"], unhex(case["achtemp"]))
+
+
+@pytest.mark.skipif(not oracle_py.reference_available(), reason="reference checkout not built here")
+@pytest.mark.parametrize("semantics", ["complex_seq", "kerseq"])
+def test_live_reference_agrees_on_fresh_inputs(semantics):
+    inp = W.make_inputs(W.Shape(11, 3, 513, 19, 4, near_pole=0.02), 99)
+    a = oracle_py.run(inp, semantics, nthreads=3)
+    b = oracle_py.run(inp, semantics, impl="ref_" + semantics)
+    for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
+        np.testing.assert_array_equal(a[k], b[k])
