@@ -1,0 +1,79 @@
+// gpp_df.cuh -- float-float ("df") arithmetic for the mixed-precision GPP
+// kernels.  A df value is the unevaluated sum h + l of two floats (~48
+// significant bits).  Building blocks are the error-free transformations
+// TwoSum (Knuth, TAOCP vol. 2, 4.2.2) and FMA-based TwoProduct (Ogita, Rump &
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).
+// Results are left unnormalised (|l| may exceed half an ulp of h): every
+// later operation consumes h and l separately, so the only rounding that is
+// not captured exactly is second order (~2^-47 of the operands).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace gpp {
+
+struct df {
+    float h, l;
+};
+
+__host__ __device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+// (a.h + a.l) * (b.h + b.l) without the l*l term.
+__host__ __device__ __forceinline__ df df_mul(df a, df b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return {p, e};
+}
+__host__ __device__ __forceinline__ df df_add(df a, df b) {
+    df s = two_sum(a.h, b.h);
+    s.l += a.l + b.l;
+    return s;
+}
+__host__ __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, {-b.h, -b.l}); }
+__host__ __device__ __forceinline__ df df_sqr(df a) {
+    const float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(a.h + a.h, a.l, e);
+    return {p, e};
+}
+// Renormalise so that |l| <= ulp(h)/2 (Fast2Sum, Dekker 1971).  Needed after
+// a cancelling subtraction, where l can be a sizeable fraction of h and the
+// l*l terms that df_mul / df_sqr drop would no longer be negligible.  The
+// exponent precondition of Fast2Sum can only fail when |h| is within a few
+// ulps of zero, where the absolute error it leaves is itself a few ulps of l.
+__host__ __device__ __forceinline__ df df_norm(df a) {
+    const float s = a.h + a.l;
+    return {s, a.l - (s - a.h)};
+}
+// 1/d for a normalised d: hardware reciprocal seed r of d.h (MUFU, relative
+// error ~2^-23) and one Newton-Raphson correction r e, e = 1 - d r computed
+// against the full df value of d; error ~2^-45.
+__host__ __device__ __forceinline__ df df_rcp(df d) {
+    float r;
+#ifdef __CUDA_ARCH__
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d.h));
+#else
+    r = 1.0f / d.h;
+#endif
+    float e = fmaf(-d.h, r, 1.0f);
+    e = fmaf(-d.l, r, e);
+    return {r, r * e};
+}
+__host__ __device__ __forceinline__ df split(double x) {
+#ifdef __CUDA_ARCH__
+    const float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+#else
+    const float h = (float)x;
+    return {h, (float)(x - (double)h)};
+#endif
+}
+__host__ __device__ __forceinline__ double to_double(df a) { return (double)a.h + (double)a.l; }
+
+}  // namespace gpp

@@ -32,26 +32,6 @@ namespace gpp {
 
 namespace {
 
-// Block-wide reduction of K doubles per thread; result in out[K] (shared).
-template <int K, int THREADS>
-__device__ __forceinline__ void block_reduce(double (&v)[K], double *red, double *out) {
-    constexpr int NWARP = THREADS / 32;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        double s = warp_sum(v[k]);
-        if (lane == 0) red[warp * K + k] = s;
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < K; k += THREADS) {
-        double s = 0.0;
-#pragma unroll
-        for (int w = 0; w < NWARP; ++w) s += red[w * K + k];
-        out[k] = s;
-    }
-    __syncthreads();
-}
-
 template <int RN, int RG, int NWC, int THREADS>
 __global__ void __launch_bounds__(THREADS)
 noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end) {
@@ -138,37 +118,8 @@ noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end) {
             }
     block_reduce<K, THREADS>(v, red, S);
 
-    // Epilogue: weight each (n1, igp) sum by 0.5 vcoul[igp] conj(aqsm[n1,igp])
-    // (gppComplex_seq.cpp:146,374,379) and add the pairs in a fixed order.
-    const long long tile = (long long)blockIdx.y * gridDim.x + blockIdx.x + part.ach_tile0;
-    const int t = threadIdx.x;
-    if (t < NWC || (part.n1 && t >= 32 && t < 32 + RN)) {
-        const bool is_n1 = t >= 32;
-        double2 tot = make_double2(0.0, 0.0);
-        const int nlo = is_n1 ? t - 32 : 0, nhi = is_n1 ? t - 32 + 1 : RN;
-        const int w = is_n1 ? 2 - iw0 : t;
-        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
-            for (int n = nlo; n < nhi; ++n) {
-                const int b = band0 + n;
-                if (b >= band_end) continue;
-#pragma unroll
-                for (int g = 0; g < RG; ++g) {
-                    const int row = row0 + g;
-                    if (row >= p.ng) continue;
-                    const int igp = resolve_igp(p, row, part.err);
-                    if (igp < 0) continue;
-                    const double2 m = __ldg(p.aqsm + (size_t)b * nc + igp);
-                    const int k = ((n * RG + g) * NWC + w) * 2;
-                    const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
-                    tot = cadd(tot, cscale(cscale(s, 0.5), __ldg(p.vcoul + igp)));
-                }
-            }
-            if (!is_n1)
-                part.ach[(long long)(iw0 + w) * part.ach_seg + tile] = tot;
-            else if (band0 + nlo < band_end)
-                part.n1[(long long)(band0 + nlo) * part.n1_seg + blockIdx.x] = tot;
-        }
-    }
+    noflag_epilogue<RN, RG, NWC>(p, part, S, row0, band0, band_end, iw0,
+                                 (long long)blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x);
 }
 
 // One occupied-band term of ssxt_scht_solver (gppComplex_seq.cpp:16-63),

@@ -113,4 +113,65 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Block-wide reduction of K doubles per thread (fixed shuffle tree within a
+// warp, fixed warp order across warps); the sums land in out[K] (shared).
+template <int K, int THREADS>
+__device__ __forceinline__ void block_reduce(double (&v)[K], double *red, double *out) {
+    constexpr int NWARP = THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = warp_sum(v[k]);
+        if (lane == 0) red[warp * K + k] = s;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += THREADS) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < NWARP; ++w) s += red[w * K + k];
+        out[k] = s;
+    }
+    __syncthreads();
+}
+
+// Epilogue of an unoccupied-band block: S holds, per (band n, row g,
+// frequency w), the ig sum of aqsn * Q * conj(wdiff) / |wdiff|^2 as
+// S[((n*RG + g)*NWC + w)*2 + {0,1}].  Weight each (n1, igp) sum by
+// 0.5 vcoul[igp] conj(aqsm[n1,igp]) (gppComplex_seq.cpp:146,374,379), add
+// the pairs in a fixed order and store one partial per frequency (threads
+// 0..NWC-1) and, for the iw = 2 column, one per band (threads 32..32+RN-1).
+template <int RN, int RG, int NWC>
+__device__ __forceinline__ void noflag_epilogue(const Problem &p, const Partials &part,
+                                                const double *S, int row0, int band0,
+                                                int band_end, int iw0, long long tile_in_launch,
+                                                int row_tile) {
+    const long long tile = tile_in_launch + part.ach_tile0;
+    const int t = threadIdx.x;
+    if (!(t < NWC || (part.n1 && t >= 32 && t < 32 + RN))) return;
+    const bool is_n1 = t >= 32;
+    const int nlo = is_n1 ? t - 32 : 0, nhi = is_n1 ? t - 32 + 1 : RN;
+    const int w = is_n1 ? 2 - iw0 : t;
+    if (w < 0 || w >= NWC || iw0 + w >= p.nw) return;
+    double2 tot = make_double2(0.0, 0.0);
+    for (int n = nlo; n < nhi; ++n) {
+        const int b = band0 + n;
+        if (b >= band_end) continue;
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const int row = row0 + g;
+            if (row >= p.ng) continue;
+            const int igp = resolve_igp(p, row, part.err);
+            if (igp < 0) continue;
+            const double2 m = __ldg(p.aqsm + (size_t)b * p.nc + igp);
+            const int k = ((n * RG + g) * NWC + w) * 2;
+            const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
+            tot = cadd(tot, cscale(cscale(s, 0.5), __ldg(p.vcoul + igp)));
+        }
+    }
+    if (!is_n1)
+        part.ach[(long long)(iw0 + w) * part.ach_seg + tile] = tot;
+    else if (band0 + nlo < band_end)
+        part.n1[(long long)(band0 + nlo) * part.n1_seg + row_tile] = tot;
+}
+
 }  // namespace gpp

@@ -1,11 +1,263 @@
-// gpp_mixed.cu -- mixed-precision unoccupied-band kernel (placeholder until
-// the float-float kernel lands).
+// gpp_mixed.cu -- mixed-precision unoccupied-band kernel of the GPP sigma
+// reduction for sm_103a.
+//
+// Why mixed precision pays on GB300: the FP64 pipe retires ~2 FMA/clk/SM
+// against ~128 FP32 FMA/clk/SM, so an FP64 operation costs as much issue time
+// as ~64 FP32 operations.  The bulk of every term therefore runs in
+// float-float ("df") arithmetic: a value is an unevaluated sum hi + lo of two
+// floats (~48 significant bits), combined with the error-free transformations
+// TwoSum (Knuth) and FMA-based TwoProduct (Dekker; Ogita, Rump & Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).  Rounding
+// errors of the main path are captured exactly; only second-order cross
+// terms round in FP32, so each term carries ~2^-44 relative error, far below
+// the 1e-8 target, while costing ~85 FP32 instructions instead of ~11 FP64
+// ones (~700 FP32-equivalents).
+//
+// FP64 is kept where stability needs it:
+//  * the input conversion: a prep pass computes Q = wtilde * I_eps in FP64 and
+//    splits wtilde, Q, aqsn and wx into float hi/lo planes once per call
+//    (memory-bound, ~1% of the kernel time), so no FP64 conversion sits in
+//    the hot loop;
+//  * near the plasmon pole, |wdiff| < 1e-3 |wx|, the whole term (wdiff, the
+//    division, the products) is recomputed in FP64 from the original inputs;
+//  * the cross-thread, cross-block and final sums (FP64 trees, fixed order).
+//
+// Work decomposition matches the FP64 kernel (RG rows x RN bands x NWC
+// frequencies per block, threads striding over ig, 16-byte vector loads) with
+// a grouped tile order so that GROUP row tiles stay resident in L2 while all
+// band tiles stream past them.
+#include "gpp_df.cuh"
 #include "gpp_kernels.h"
 
 namespace gpp {
-size_t mixed_split_bytes(const Problem &) { return 0; }
-TileShape mixed_noflag_shape(const Problem &p) { return fp64_noflag_shape(p); }
-cudaError_t launch_mixed_noflag(const Problem &, const Partials &, void *, int, int, cudaStream_t) {
-    return cudaErrorNotSupported;
+
+namespace {
+
+// Split planes written by the prep kernels (all float4 = 16 bytes).
+struct SplitPlanes {
+    float4 *rowW;  // [ng][nc]: wt.re hi, lo, wt.im hi, lo
+    float4 *rowQ;  // [ng][nc]: (wt*I_eps).re hi, lo, .im hi, lo
+    float4 *band;  // [nb][nc]: aqsn.re hi, lo, .im hi, lo
+    float2 *wx;    // [nb][nw]: wx hi, lo
+};
+
+SplitPlanes planes(const Problem &p, void *ws) {
+    char *w = static_cast<char *>(ws);
+    SplitPlanes s;
+    const size_t rows = (size_t)p.ng * p.nc, bands = (size_t)p.nb * p.nc;
+    s.rowW = reinterpret_cast<float4 *>(w);
+    s.rowQ = s.rowW + rows;
+    s.band = s.rowQ + rows;
+    s.wx = reinterpret_cast<float2 *>(s.band + bands);
+    return s;
 }
+
+__global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s) {
+    const size_t n = (size_t)p.ng * p.nc;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const double2 wt = __ldg(p.wt + i);
+        const double2 ie = __ldg(p.ieps + i);
+        const double2 q = cmul(wt, ie);
+        const df wr = split(wt.x), wi = split(wt.y), qr = split(q.x), qi = split(q.y);
+        s.rowW[i] = make_float4(wr.h, wr.l, wi.h, wi.l);
+        s.rowQ[i] = make_float4(qr.h, qr.l, qi.h, qi.l);
+    }
+}
+
+__global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes s, int b0,
+                                                          int b1) {
+    const size_t n = (size_t)(b1 - b0) * p.nc;
+    const size_t base = (size_t)b0 * p.nc;
+    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
+        const double2 a = __ldg(p.aqsn + base + i);
+        const df ar = split(a.x), ai = split(a.y);
+        s.band[base + i] = make_float4(ar.h, ar.l, ai.h, ai.l);
+    }
+    const int nwx = (b1 - b0) * p.nw;
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < nwx; i += gridDim.x * 256) {
+        const int b = b0 + i / p.nw, iw = i % p.nw;
+        const df x = split(__ldg(p.wx + (size_t)b * p.wx_stride + iw));
+        s.wx[(size_t)b * p.nw + iw] = make_float2(x.h, x.l);
+    }
+}
+
+// The full term in FP64 from the original inputs, for |wdiff| < 1e-3 |wx|.
+__device__ __noinline__ void pole_term_fp64(const Problem &p, int row, int band, int ig, int iw,
+                                            df &re, df &im) {
+    const double2 wt = __ldg(p.wt + (size_t)row * p.nc + ig);
+    const double2 ie = __ldg(p.ieps + (size_t)row * p.nc + ig);
+    const double2 a = __ldg(p.aqsn + (size_t)band * p.nc + ig);
+    const double wx = __ldg(p.wx + (size_t)band * p.wx_stride + iw);
+    const double2 A = cmul(a, cmul(wt, ie));
+    const double wr = wx - wt.x;
+    const double r = 1.0 / (wr * wr + wt.y * wt.y);
+    const double tx = (A.x * wr - A.y * wt.y) * r;
+    const double ty = (A.y * wr + A.x * wt.y) * r;
+    re = split(tx);
+    im = split(ty);
+}
+
+template <int RN, int RG, int NWC, int THREADS, int GROUP>
+__global__ void __launch_bounds__(THREADS)
+mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
+                    int row_tiles, int band_tiles) {
+    constexpr int K = RN * RG * NWC * 2;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+
+    // Grouped tile order: GROUP consecutive row tiles share each band tile.
+    const int tiles_per_group = GROUP * band_tiles;
+    const int grp = blockIdx.x / tiles_per_group;
+    const int in_grp = blockIdx.x - grp * tiles_per_group;
+    const int rows_in_grp = min(GROUP, row_tiles - grp * GROUP);
+    const int row_tile = grp * GROUP + in_grp % rows_in_grp;
+    const int band_tile = in_grp / rows_in_grp;
+    const int row0 = row_tile * RG;
+    const int band0 = band_begin + band_tile * RN;
+    const int iw0 = blockIdx.y * NWC;
+    const int nc = p.nc;
+
+    const float4 *rw[RG];
+    const float4 *rq[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const int r = min(row0 + g, p.ng - 1);
+        rw[g] = s.rowW + (size_t)r * nc;
+        rq[g] = s.rowQ + (size_t)r * nc;
+    }
+    const float4 *nb[RN];
+    df wx[RN][NWC];
+    float pole_thr[RN][NWC];
+#pragma unroll
+    for (int n = 0; n < RN; ++n) {
+        const int b = min(band0 + n, band_end - 1);
+        nb[n] = s.band + (size_t)b * nc;
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
+            wx[n][w] = {x.x, x.y};
+            pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
+        }
+    }
+
+    df acc[RN][RG][NWC][2];
+#pragma unroll
+    for (int n = 0; n < RN; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                acc[n][g][w][0] = {0.f, 0.f};
+                acc[n][g][w][1] = {0.f, 0.f};
+            }
+
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const float4 a = __ldg(rw[g] + ig);
+            const float4 b = __ldg(rq[g] + ig);
+            wtr[g] = {a.x, a.y};
+            wti[g] = {a.z, a.w};
+            qr[g] = {b.x, b.y};
+            qi[g] = {b.z, b.w};
+            wti2[g] = df_sqr(wti[g]);
+        }
+#pragma unroll
+        for (int n = 0; n < RN; ++n) {
+            const float4 av = __ldg(nb[n] + ig);
+            const df ar = {av.x, av.y}, ai = {av.z, av.w};
+#pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                // A = aqsn * Q (frequency independent)
+                const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
+                const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
+                const df Ai_wti = df_mul(Ai, wti[g]);
+                const df Ar_wti = df_mul(Ar, wti[g]);
+#pragma unroll
+                for (int w = 0; w < NWC; ++w) {
+                    const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
+                    const df d = df_add(df_sqr(wr), wti2[g]);      // |wdiff|^2
+                    df tre, tim;
+                    if (d.h >= pole_thr[n][w]) {
+                        const df r = df_rcp(d);
+                        // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
+                        tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
+                        tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
+                    } else {
+                        pole_term_fp64(p, min(row0 + g, p.ng - 1), min(band0 + n, band_end - 1),
+                                       ig, min(iw0 + w, p.nw - 1), tre, tim);
+                    }
+                    acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
+                    acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
+                }
+            }
+        }
+    }
+
+    double v[K];
+#pragma unroll
+    for (int n = 0; n < RN; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const int k = ((n * RG + g) * NWC + w) * 2;
+                v[k] = to_double(acc[n][g][w][0]);
+                v[k + 1] = to_double(acc[n][g][w][1]);
+            }
+    block_reduce<K, THREADS>(v, red, S);
+    noflag_epilogue<RN, RG, NWC>(p, part, S, row0, band0, band_end, iw0,
+                                 (long long)band_tile * row_tiles + row_tile, row_tile);
+}
+
+constexpr int kGroup = 16;
+
+template <int RN, int RG, int NWC, int THREADS>
+cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
+                           int b1, cudaStream_t st) {
+    const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, RN);
+    dim3 grid((unsigned)row_tiles * band_tiles, ceil_div(p.nw, NWC));
+    mixed_noflag_kernel<RN, RG, NWC, THREADS, kGroup>
+        <<<grid, THREADS, 0, st>>>(p, part, s, b0, b1, row_tiles, band_tiles);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+static int nwc_for(int nw) { return nw <= 4 ? nw : 8; }
+
+TileShape mixed_noflag_shape(const Problem &p) {
+    const int nwc = nwc_for(p.nw);
+    return nwc <= 4 ? TileShape{4, 2, nwc, 128} : TileShape{2, 2, nwc, 128};
+}
+
+size_t mixed_split_bytes(const Problem &p) {
+    return sizeof(float4) * ((size_t)2 * p.ng * p.nc + (size_t)p.nb * p.nc) +
+           sizeof(float2) * (size_t)p.nb * p.nw;
+}
+
+cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws, int b0,
+                                int b1, cudaStream_t st) {
+    if (b1 <= b0 || p.ng == 0) return cudaSuccess;
+    const SplitPlanes s = planes(p, split_ws);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms > 0 ? sms * 8 : 1024;
+    split_rows_kernel<<<blocks, 256, 0, st>>>(p, s);
+    split_bands_kernel<<<blocks, 256, 0, st>>>(p, s, b0, b1);
+    count_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    switch (nwc_for(p.nw)) {
+        case 1: return launch_mixed_t<4, 2, 1, 128>(p, part, s, b0, b1, st);
+        case 2: return launch_mixed_t<4, 2, 2, 128>(p, part, s, b0, b1, st);
+        case 3: return launch_mixed_t<4, 2, 3, 128>(p, part, s, b0, b1, st);
+        case 4: return launch_mixed_t<4, 2, 4, 128>(p, part, s, b0, b1, st);
+        default: return launch_mixed_t<2, 2, 8, 128>(p, part, s, b0, b1, st);
+    }
+}
+
 }  // namespace gpp

@@ -12,6 +12,6 @@ __all__ = ["build", "capi", "workload", "ops"]
 
 def __getattr__(name):
     if name == "ops":
-        from . import ops
-        return ops
+        import importlib
+        return importlib.import_module(__name__ + ".ops")
     raise AttributeError(name)

@@ -1,0 +1,56 @@
+"""Run the GPP sigma reduction on one synthetic workload from the command line.
+
+    python doe-csfg-hackathon_gb300/gppsigma/run_case.py --workload profile \
+        --precision mixed --repeat 3
+
+Generates the seeded inputs, copies them to cuda:0, runs gpp_sigma `--repeat`
+times (synchronising and checking device-side faults) and prints achtemp.
+Useful as a fixed command line for profilers.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from gppsigma import workload as W  # noqa: E402
+
+# Extra shapes for profiling: larger than L2 (129 MB), a few hundred MB total.
+SHAPES = dict(W.CONFIGS)
+SHAPES["profile"] = W.Shape(512, 2, 8192, 512, 3, near_pole=0.01)
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="profile", choices=sorted(SHAPES))
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--semantics", default="complex_seq", choices=["complex_seq", "kerseq"])
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=20240607)
+    args = ap.parse_args()
+
+    import torch
+    from gppsigma import ops
+
+    torch.cuda.set_device(0)
+    inp = W.make_inputs(SHAPES[args.workload], args.seed)
+    d = ops.DeviceInputs.from_host(inp)
+    out = None
+    for i in range(args.repeat):
+        t0 = time.perf_counter()
+        out = ops.sigma(d, args.precision, args.semantics, out=out)
+        ops.wait()
+        dt = time.perf_counter() - t0
+        print(f"step {i}: {dt * 1e3:.2f} ms, {inp.shape.terms / dt:.4e} terms/s")
+    for iw, z in enumerate(out.achtemp.cpu().numpy()):
+        print(f"achtemp[{iw}] = ({z.real:.15g},{z.imag:.15g})")
+    for iw, z in enumerate(out.asxtemp.cpu().numpy()):
+        print(f"asxtemp[{iw}] = ({z.real:.15g},{z.imag:.15g})")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

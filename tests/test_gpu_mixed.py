@@ -1,0 +1,81 @@
+"""Mixed-precision (float-float bulk, FP64 near the pole) path: error against
+the reference fixtures and against the FP64 kernel on the same inputs."""
+import numpy as np
+import pytest
+
+from conftest import case_inputs, load_golden, rel_err, unhex
+from gppsigma import build, capi, workload as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+MIXED_TOL = 1e-8  # per real/imaginary component, relative to the FP64 result
+CASES = [c for c in load_golden() if c["kind"] == "seeded"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    build.build()
+    capi.load()
+
+
+def ops():
+    from gppsigma import ops as o
+    return o
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+def test_mixed_matches_reference_fixture(case):
+    o = ops()
+    inp = case_inputs(case)
+    d = o.DeviceInputs.from_host(inp)
+    res = o.sigma(d, "mixed", case["semantics"], acht_n1=inp.shape.nw >= 3, achstemp=True)
+    o.wait()
+    assert rel_err(res.achtemp.cpu().numpy(), unhex(case["achtemp"])) <= MIXED_TOL
+    assert rel_err(res.asxtemp.cpu().numpy(), unhex(case["asxtemp"])) <= MIXED_TOL
+    if res.acht_n1_loc is not None:
+        want = unhex(case["acht_n1_loc"])
+        err = np.max(np.abs(res.acht_n1_loc.cpu().numpy() - want))
+        assert err <= MIXED_TOL * max(np.max(np.abs(want)), 1e-300)
+
+
+@pytest.mark.parametrize("shape", [
+    W.Shape(32, 2, 4096, 64, 3, near_pole=0.01),
+    W.Shape(16, 2, 2048, 40, 3, near_pole=0.2),
+    W.Shape(12, 3, 3000, 33, 32, dw=0.25, near_pole=0.01),
+    W.Shape(10, 2, 1000, 17, 2),
+], ids=["near_pole_1pct", "near_pole_20pct", "sweep32", "two_freq"])
+def test_mixed_vs_fp64_kernel(shape):
+    o = ops()
+    d = o.DeviceInputs.from_host(W.make_inputs(shape, 77))
+    a = o.sigma(d, "fp64", acht_n1=shape.nw >= 3)
+    b = o.sigma(d, "mixed", acht_n1=shape.nw >= 3)
+    o.wait()
+    assert rel_err(b.achtemp.cpu().numpy(), a.achtemp.cpu().numpy()) <= MIXED_TOL
+    assert rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy()) <= MIXED_TOL
+
+
+def test_mixed_bit_reproducible():
+    o = ops()
+    d = o.DeviceInputs.from_host(W.make_inputs(W.Shape(40, 2, 4096, 80, 3, near_pole=0.01), 5))
+    a = o.sigma(d, "mixed")
+    b = o.sigma(d, "mixed")
+    o.wait()
+    assert torch.equal(torch.view_as_real(a.achtemp), torch.view_as_real(b.achtemp))
+
+
+def test_production_near_pole_mixed_within_1e8_of_fp64():
+    """The headline claim at full size: 512 bands, ncouls 32768, ngpown 1638,
+    1% of wtilde next to a wx value."""
+    o = ops()
+    inp = W.make_inputs(W.CONFIGS["production_near_pole"], 20240607)
+    d = o.DeviceInputs.from_host(inp)
+    a = o.sigma(d, "fp64")
+    b = o.sigma(d, "mixed")
+    o.wait()
+    ea = rel_err(b.achtemp.cpu().numpy(), a.achtemp.cpu().numpy())
+    ex = rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy())
+    print(f"mixed vs fp64: achtemp {ea:.3e}, asxtemp {ex:.3e}")
+    assert ea <= MIXED_TOL and ex <= MIXED_TOL
