@@ -16,15 +16,41 @@ struct df {
     float h, l;
 };
 
+// Additions and products that the compiler must not fuse into FMAs: nvcc
+// contracts a*b + c by default, which would silently break the error-free
+// transformations below (TwoSum relies on s = fl(a + b) of the already
+// rounded operands).  The _rn intrinsics are never contracted.
+__host__ __device__ __forceinline__ float fadd(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float fsub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+__host__ __device__ __forceinline__ float fmul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+
 __host__ __device__ __forceinline__ df two_sum(float a, float b) {
-    const float s = a + b;
-    const float bb = s - a;
-    const float e = (a - (s - bb)) + (b - bb);
+    const float s = fadd(a, b);
+    const float bb = fsub(s, a);
+    const float e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
     return {s, e};
 }
 // (a.h + a.l) * (b.h + b.l) without the l*l term.
 __host__ __device__ __forceinline__ df df_mul(df a, df b) {
-    const float p = a.h * b.h;
+    const float p = fmul(a.h, b.h);
     float e = fmaf(a.h, b.h, -p);
     e = fmaf(a.h, b.l, e);
     e = fmaf(a.l, b.h, e);
@@ -32,14 +58,14 @@ __host__ __device__ __forceinline__ df df_mul(df a, df b) {
 }
 __host__ __device__ __forceinline__ df df_add(df a, df b) {
     df s = two_sum(a.h, b.h);
-    s.l += a.l + b.l;
+    s.l = fadd(s.l, fadd(a.l, b.l));
     return s;
 }
 __host__ __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, {-b.h, -b.l}); }
 __host__ __device__ __forceinline__ df df_sqr(df a) {
-    const float p = a.h * a.h;
+    const float p = fmul(a.h, a.h);
     float e = fmaf(a.h, a.h, -p);
-    e = fmaf(a.h + a.h, a.l, e);
+    e = fmaf(fadd(a.h, a.h), a.l, e);
     return {p, e};
 }
 // Renormalise so that |l| <= ulp(h)/2 (Fast2Sum, Dekker 1971).  Needed after
@@ -48,8 +74,8 @@ __host__ __device__ __forceinline__ df df_sqr(df a) {
 // exponent precondition of Fast2Sum can only fail when |h| is within a few
 // ulps of zero, where the absolute error it leaves is itself a few ulps of l.
 __host__ __device__ __forceinline__ df df_norm(df a) {
-    const float s = a.h + a.l;
-    return {s, a.l - (s - a.h)};
+    const float s = fadd(a.h, a.l);
+    return {s, fsub(a.l, fsub(s, a.h))};
 }
 // 1/d for a normalised d: hardware reciprocal seed r of d.h (MUFU, relative
 // error ~2^-23) and one Newton-Raphson correction r e, e = 1 - d r computed
@@ -63,7 +89,7 @@ __host__ __device__ __forceinline__ df df_rcp(df d) {
 #endif
     float e = fmaf(-d.h, r, 1.0f);
     e = fmaf(-d.l, r, e);
-    return {r, r * e};
+    return {r, fmul(r, e)};
 }
 __host__ __device__ __forceinline__ df split(double x) {
 #ifdef __CUDA_ARCH__
