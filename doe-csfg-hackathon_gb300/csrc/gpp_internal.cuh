@@ -24,7 +24,11 @@ constexpr double kLimitTwo = 0.25;  // pow(0.5, 2)
 enum : int { kSemComplexSeq = 0, kSemKerSeq = 1 };
 
 // Device-side fault bits (workspace word, read by gpp_wait).
-enum : int { kErrBadIgp = 1, kErrBadIndinv = 2 };
+enum : int { kErrBadIgp = 1, kErrBadIndinv = 2, kErrPipelineTimeout = 4 };
+
+// Iteration cap of every device-side wait (mbarrier polls): a wait that runs
+// out raises kErrPipelineTimeout and the block abandons its tile.
+constexpr int kWaitLimit = 1 << 22;
 
 // Everything a sigma kernel needs about one problem (one quasiparticle
 // state).  Passed by value as a kernel parameter or read from a table by the

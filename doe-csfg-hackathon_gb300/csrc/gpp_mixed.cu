@@ -97,15 +97,68 @@ __device__ __noinline__ void pole_term_fp64(const Problem &p, int row, int band,
     im = split(ty);
 }
 
-template <int RN, int RG, int NWC, int THREADS, int GROUP>
-__global__ void __launch_bounds__(THREADS)
+// ---------------------------------------------------------------------------
+// Shared-memory pipeline primitives: 1-D bulk TMA copies (cp.async.bulk)
+// completing on an mbarrier with a transaction count.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for phase `parity` of `bar`; false after kWaitLimit polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+    for (int it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes,
+                                              unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Unoccupied bands, mixed precision.  A block owns RG local G' rows and
+// NWARP * RNW bands; warp w owns bands band0 + w*RNW .. +RNW-1.  The ig range
+// is processed in chunks of KC columns: thread 0 streams each chunk's row
+// planes (wtilde, Q: RG x KC x 16 B each) and band planes (aqsn: NWARP*RNW x
+// KC x 16 B) into a double-buffered shared-memory stage with 1-D bulk TMA
+// copies; every warp then reads the rows from shared memory (one copy serves
+// all warps) and its own bands, lanes on consecutive ig (conflict-free 16-byte
+// LDS).  Per-lane df sums are reduced across the warp with a fixed shuffle
+// tree in df arithmetic, converted to FP64 once, and combined by the common
+// epilogue.
+template <int RNW, int RG, int NWC, int NWARP, int KC, int GROUP>
+__global__ void __launch_bounds__(NWARP * 32)
 mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
                     int row_tiles, int band_tiles) {
-    constexpr int K = RN * RG * NWC * 2;
-    __shared__ double red[(THREADS / 32) * K];
+    constexpr int BN = NWARP * RNW;           // bands per block
+    constexpr int K = BN * RG * NWC * 2;      // doubles in the block result
+    constexpr int STAGE = (2 * RG + BN) * KC; // float4 per stage
+    static_assert(KC % 32 == 0, "chunk must be a multiple of the warp width");
+    extern __shared__ __align__(128) float4 stage_mem[];
+    __shared__ unsigned long long bars[2];
     __shared__ double S[K];
 
-    // Grouped tile order: GROUP consecutive row tiles share each band tile.
     const int tiles_per_group = GROUP * band_tiles;
     const int grp = blockIdx.x / tiles_per_group;
     const int in_grp = blockIdx.x - grp * tiles_per_group;
@@ -113,25 +166,49 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
     const int row_tile = grp * GROUP + in_grp % rows_in_grp;
     const int band_tile = in_grp / rows_in_grp;
     const int row0 = row_tile * RG;
-    const int band0 = band_begin + band_tile * RN;
+    const int band0 = band_begin + band_tile * BN;
     const int iw0 = blockIdx.y * NWC;
     const int nc = p.nc;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunks = (nc + KC - 1) / KC;
 
-    const float4 *rw[RG];
-    const float4 *rq[RG];
+    // Producer: copy chunk c into stage (c & 1).
+    auto issue = [&](int c) {
+        const int k0 = c * KC;
+        const int cnt = min(KC, nc - k0);
+        const unsigned bytes = (unsigned)cnt * 16u;
+        float4 *st = stage_mem + (c & 1) * STAGE;
+        unsigned long long *bar = &bars[c & 1];
+        mbar_expect_tx(bar, bytes * (2 * RG + BN));
 #pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        const int r = min(row0 + g, p.ng - 1);
-        rw[g] = s.rowW + (size_t)r * nc;
-        rq[g] = s.rowQ + (size_t)r * nc;
+        for (int g = 0; g < RG; ++g) {
+            const size_t r = (size_t)min(row0 + g, p.ng - 1) * nc + k0;
+            bulk_copy_g2s(st + g * KC, s.rowW + r, bytes, bar);
+            bulk_copy_g2s(st + (RG + g) * KC, s.rowQ + r, bytes, bar);
+        }
+#pragma unroll
+        for (int n = 0; n < BN; ++n) {
+            const size_t b = (size_t)min(band0 + n, band_end - 1) * nc + k0;
+            bulk_copy_g2s(st + (2 * RG + n) * KC, s.band + b, bytes, bar);
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    const float4 *nb[RN];
-    df wx[RN][NWC];
-    float pole_thr[RN][NWC];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        issue(0);
+        if (nchunks > 1) issue(1);
+    }
+
+    df wx[RNW][NWC];
+    float pole_thr[RNW][NWC];
 #pragma unroll
-    for (int n = 0; n < RN; ++n) {
-        const int b = min(band0 + n, band_end - 1);
-        nb[n] = s.band + (size_t)b * nc;
+    for (int n = 0; n < RNW; ++n) {
+        const int b = min(band0 + warp * RNW + n, band_end - 1);
 #pragma unroll
         for (int w = 0; w < NWC; ++w) {
             const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
@@ -139,10 +216,9 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
             pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
         }
     }
-
-    df acc[RN][RG][NWC][2];
+    df acc[RNW][RG][NWC][2];
 #pragma unroll
-    for (int n = 0; n < RN; ++n)
+    for (int n = 0; n < RNW; ++n)
 #pragma unroll
         for (int g = 0; g < RG; ++g)
 #pragma unroll
@@ -151,75 +227,123 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
                 acc[n][g][w][1] = {0.f, 0.f};
             }
 
-    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
-        df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
-#pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            const float4 a = __ldg(rw[g] + ig);
-            const float4 b = __ldg(rq[g] + ig);
-            wtr[g] = {a.x, a.y};
-            wti[g] = {a.z, a.w};
-            qr[g] = {b.x, b.y};
-            qi[g] = {b.z, b.w};
-            wti2[g] = df_sqr(wti[g]);
+    bool timed_out = false;
+    unsigned parity[2] = {0u, 0u};
+    for (int c = 0; c < nchunks; ++c) {
+        const int sidx = c & 1;
+        const bool ok = mbar_wait(&bars[sidx], parity[sidx]);
+        parity[sidx] ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
         }
-#pragma unroll
-        for (int n = 0; n < RN; ++n) {
-            const float4 av = __ldg(nb[n] + ig);
-            const df ar = {av.x, av.y}, ai = {av.z, av.w};
+        const float4 *st = stage_mem + sidx * STAGE;
+        const int k0 = c * KC;
+        const int cnt = min(KC, nc - k0);
+#pragma unroll 1
+        for (int il = lane; il < cnt; il += 32) {
+            df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
 #pragma unroll
             for (int g = 0; g < RG; ++g) {
-                // A = aqsn * Q (frequency independent)
-                const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
-                const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
-                const df Ai_wti = df_mul(Ai, wti[g]);
-                const df Ar_wti = df_mul(Ar, wti[g]);
+                const float4 wv = st[g * KC + il];
+                const float4 qv = st[(RG + g) * KC + il];
+                wtr[g] = {wv.x, wv.y};
+                wti[g] = {wv.z, wv.w};
+                qr[g] = {qv.x, qv.y};
+                qi[g] = {qv.z, qv.w};
+                wti2[g] = df_sqr(wti[g]);
+            }
 #pragma unroll
-                for (int w = 0; w < NWC; ++w) {
-                    const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
-                    const df d = df_add(df_sqr(wr), wti2[g]);      // |wdiff|^2
-                    df tre, tim;
-                    if (d.h >= pole_thr[n][w]) {
-                        const df r = df_rcp(d);
-                        // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
-                        tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
-                        tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
-                    } else {
-                        pole_term_fp64(p, min(row0 + g, p.ng - 1), min(band0 + n, band_end - 1),
-                                       ig, min(iw0 + w, p.nw - 1), tre, tim);
+            for (int n = 0; n < RNW; ++n) {
+                const float4 av = st[(2 * RG + warp * RNW + n) * KC + il];
+                const df ar = {av.x, av.y}, ai = {av.z, av.w};
+#pragma unroll
+                for (int g = 0; g < RG; ++g) {
+                    // A = aqsn * Q (frequency independent)
+                    const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
+                    const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
+                    const df Ai_wti = df_mul(Ai, wti[g]);
+                    const df Ar_wti = df_mul(Ar, wti[g]);
+#pragma unroll
+                    for (int w = 0; w < NWC; ++w) {
+                        const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
+                        const df d = df_add(df_sqr(wr), wti2[g]);         // |wdiff|^2
+                        df tre, tim;
+                        if (d.h >= pole_thr[n][w]) {
+                            const df r = df_rcp(d);
+                            // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
+                            tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
+                            tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
+                        } else {
+                            pole_term_fp64(p, min(row0 + g, p.ng - 1),
+                                           min(band0 + warp * RNW + n, band_end - 1), k0 + il,
+                                           min(iw0 + w, p.nw - 1), tre, tim);
+                        }
+                        acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
+                        acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
                     }
-                    acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
-                    acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
                 }
             }
         }
+        __syncthreads();  // every warp is done with this stage
+        if (threadIdx.x == 0 && c + 2 < nchunks) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(c + 2);
+        }
     }
 
-    double v[K];
+    if (timed_out) {
+        if (threadIdx.x == 0) {
+            atomicOr(part.err, kErrPipelineTimeout);
+            // Let copies still in flight land before the block retires.
+            for (int b = 0; b < 2; ++b) mbar_wait(&bars[b], parity[b]);
+        }
+        return;
+    }
+
+    // Warp tree in df arithmetic (fixed order), then one FP64 value per
+    // (band, row, frequency) and component into shared memory.
 #pragma unroll
-    for (int n = 0; n < RN; ++n)
+    for (int n = 0; n < RNW; ++n)
 #pragma unroll
         for (int g = 0; g < RG; ++g)
 #pragma unroll
-            for (int w = 0; w < NWC; ++w) {
-                const int k = ((n * RG + g) * NWC + w) * 2;
-                v[k] = to_double(acc[n][g][w][0]);
-                v[k + 1] = to_double(acc[n][g][w][1]);
-            }
-    block_reduce<K, THREADS>(v, red, S);
-    noflag_epilogue<RN, RG, NWC>(p, part, S, row0, band0, band_end, iw0,
+            for (int w = 0; w < NWC; ++w)
+#pragma unroll
+                for (int ri = 0; ri < 2; ++ri) {
+                    df v = acc[n][g][w][ri];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const df o = {__shfl_down_sync(0xffffffffu, v.h, off),
+                                      __shfl_down_sync(0xffffffffu, v.l, off)};
+                        v = df_add(v, o);
+                    }
+                    if (lane == 0)
+                        S[(((warp * RNW + n) * RG + g) * NWC + w) * 2 + ri] = to_double(v);
+                }
+    __syncthreads();
+    noflag_epilogue<BN, RG, NWC>(p, part, S, row0, band0, band_end, iw0,
                                  (long long)band_tile * row_tiles + row_tile, row_tile);
 }
 
 constexpr int kGroup = 16;
+constexpr int kWarps = 4;
+constexpr int kChunk = 128;
 
-template <int RN, int RG, int NWC, int THREADS>
+template <int RNW, int RG, int NWC>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
                            int b1, cudaStream_t st) {
-    const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, RN);
+    constexpr int BN = kWarps * RNW;
+    const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
+    const size_t smem = sizeof(float4) * 2 * (2 * RG + BN) * kChunk;
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, kChunk, kGroup>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     dim3 grid((unsigned)row_tiles * band_tiles, ceil_div(p.nw, NWC));
-    mixed_noflag_kernel<RN, RG, NWC, THREADS, kGroup>
-        <<<grid, THREADS, 0, st>>>(p, part, s, b0, b1, row_tiles, band_tiles);
+    kern<<<grid, kWarps * 32, smem, st>>>(p, part, s, b0, b1, row_tiles, band_tiles);
     count_launch();
     return cudaGetLastError();
 }
@@ -228,9 +352,13 @@ cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPl
 
 static int nwc_for(int nw) { return nw <= 4 ? nw : 8; }
 
+// Rows per block for a frequency chunk: 2 rows x 4 frequencies keeps the df
+// accumulators (RG * NWC * 2 values of 2 floats) within ~100 registers.
+static int mixed_rg(int nwc) { return nwc <= 4 ? 2 : 1; }
+
 TileShape mixed_noflag_shape(const Problem &p) {
     const int nwc = nwc_for(p.nw);
-    return nwc <= 4 ? TileShape{4, 2, nwc, 128} : TileShape{2, 2, nwc, 128};
+    return TileShape{kWarps, mixed_rg(nwc), nwc, kWarps * 32};
 }
 
 size_t mixed_split_bytes(const Problem &p) {
@@ -252,11 +380,11 @@ cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *sp
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_mixed_t<4, 2, 1, 128>(p, part, s, b0, b1, st);
-        case 2: return launch_mixed_t<4, 2, 2, 128>(p, part, s, b0, b1, st);
-        case 3: return launch_mixed_t<4, 2, 3, 128>(p, part, s, b0, b1, st);
-        case 4: return launch_mixed_t<4, 2, 4, 128>(p, part, s, b0, b1, st);
-        default: return launch_mixed_t<2, 2, 8, 128>(p, part, s, b0, b1, st);
+        case 1: return launch_mixed_t<1, 2, 1>(p, part, s, b0, b1, st);
+        case 2: return launch_mixed_t<1, 2, 2>(p, part, s, b0, b1, st);
+        case 3: return launch_mixed_t<1, 2, 3>(p, part, s, b0, b1, st);
+        case 4: return launch_mixed_t<1, 2, 4>(p, part, s, b0, b1, st);
+        default: return launch_mixed_t<1, 1, 8>(p, part, s, b0, b1, st);
     }
 }
 
