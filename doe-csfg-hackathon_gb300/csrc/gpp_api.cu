@@ -26,6 +26,12 @@ thread_local bool t_timed = false;
 
 void count_launch(int n) { t_launches += (unsigned long long)n; }
 
+// Records `msg` as this thread's gpp_last_error_message and returns `s`.
+gpp_status set_error(gpp_status s, const char *msg) {
+    t_err = msg ? msg : "";
+    return s;
+}
+
 namespace {
 
 gpp_status fail(gpp_status s, const char *fmt, ...) {

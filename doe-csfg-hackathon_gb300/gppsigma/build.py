@@ -26,7 +26,8 @@ LIB = os.path.join(LIBDIR, "libgpp_gb300.so")
 DRIVER = os.path.join(LIBDIR, "gpp_driver.ex")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-LIB_SOURCES = ["gpp_api.cu", "gpp_fp64.cu", "gpp_mixed.cu", "gpp_batched.cu", "gpp_compat.cpp"]
+LIB_SOURCES = ["gpp_api.cu", "gpp_fp64.cu", "gpp_mixed.cu", "gpp_batched.cu", "gpp_static.cu",
+               "gpp_compat.cpp"]
 DRIVER_SOURCES = ["gpp_driver.cpp"]
 
 

@@ -51,6 +51,7 @@ _SIGS = {
     "gpp_context_destroy": (_i, [_vp]),
     "gpp_sigma_host": (_i, [_vp, C.POINTER(GppProblem), C.POINTER(GppOutputs)]),
     "gpp_sigma_batched": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _i, _vp]),
+    "gpp_sigma_static_scratch": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _vp]),
     "gpp_last_error_message": (C.c_char_p, []),
     "gpp_launch_count": (C.c_ulonglong, []),
     "gpp_reset_launch_count": (None, []),

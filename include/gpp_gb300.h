@@ -168,6 +168,21 @@ gpp_status gpp_context_create(gpp_context **ctx);
 gpp_status gpp_context_destroy(gpp_context *ctx);
 gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gpp_outputs *out);
 
+/* No counterpart in the reference.  gpp_sigma for callers that cannot
+ * allocate device memory -- applications that have handed the GPU's memory
+ * to their own arena or to another runtime, or that cannot afford
+ * cudaMalloc's device-wide synchronisation mid-step.  It runs the same FP64
+ * kernels as gpp_sigma but keeps the block partials in a fixed 8 MiB array in
+ * the library's device image (resident on every GPU that loads the library),
+ * so it allocates nothing.  FP64 only; achtemp and asxtemp only (acht_n1_loc
+ * and achstemp must be NULL); problems needing more than 8 MiB of partials
+ * (the production shape needs ~5 MiB) return GPP_ERR_UNSUPPORTED.  All calls
+ * share the array: calls whose GPU work overlaps in time race, so serialise
+ * them on one stream.  The first call on a device looks up the array's
+ * address; make it before any stream capture. */
+gpp_status gpp_sigma_static_scratch(const gpp_problem *problem, const gpp_outputs *out,
+                                    gpp_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Batched states: many independent quasiparticle states (uneven sizes) in
  * one persistent launch over a work queue of (state, band tile, row tile).
