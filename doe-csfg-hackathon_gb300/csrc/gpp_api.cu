@@ -149,6 +149,34 @@ struct OutSpec {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Per host thread and device: a highest-priority side stream plus fork/join
+// events.  The mixed path runs the FP64 occupied-band kernel there, beside the
+// FP32 unoccupied-band kernel: the two keep different pipes busy on the same
+// SMs.  Fork and join are stream-ordered, so the pair is also captured
+// correctly into a CUDA graph.
+struct SideStream {
+    int dev = -1;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+thread_local SideStream t_side;
+
+gpp_status side_stream(int dev, SideStream **out) {
+    if (t_side.dev != dev) {
+        int lo = 0, hi = 0;
+        GPP_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
+        SideStream n;
+        GPP_CUDA_TRY(cudaStreamCreateWithPriority(&n.st, cudaStreamNonBlocking, hi),
+                     "cudaStreamCreateWithPriority");
+        GPP_CUDA_TRY(cudaEventCreateWithFlags(&n.fork, cudaEventDisableTiming), "cudaEventCreate");
+        GPP_CUDA_TRY(cudaEventCreateWithFlags(&n.join, cudaEventDisableTiming), "cudaEventCreate");
+        n.dev = dev;
+        t_side = n;  // a stream of a previously used device is kept alive
+    }
+    *out = &t_side;
+    return GPP_OK;
+}
+
 // Runs the bands [b0, b1) of problem p: occupied bands (< nv) through the
 // flag kernel, the rest through the FP64 or mixed unoccupied kernel, then
 // reduces all block partials in a fixed order into the outputs.
@@ -209,7 +237,17 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         // Different row tilings: pad the shorter per-band segments with zeros.
         e = cudaMemsetAsync(part.n1, 0, sizeof(double2) * (size_t)(n1_seg * p.nb), s);
     }
-    if (e == cudaSuccess && has_flag) {
+    SideStream *side = nullptr;
+    const bool overlap = mixed && has_flag;
+    if (overlap) {
+        st = side_stream(dev, &side);
+        if (st != GPP_OK) {
+            cudaFreeAsync(ws, s);
+            return st;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(side->fork, s);
+    }
+    if (e == cudaSuccess && has_flag && !overlap) {
         part.ach_tile0 = 0;
         e = launch_flag_fp64(p, part, s);
     }
@@ -222,6 +260,13 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
             cudaEventRecord(t_ev1, s);
             t_timed = true;
         }
+    }
+    if (e == cudaSuccess && overlap) {
+        e = cudaStreamWaitEvent(side->st, side->fork, 0);
+        part.ach_tile0 = 0;
+        if (e == cudaSuccess) e = launch_flag_fp64(p, part, side->st);
+        if (e == cudaSuccess) e = cudaEventRecord(side->join, side->st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, side->join, 0);
     }
     if (e == cudaSuccess && want_achs)
         e = launch_achstemp(p, reinterpret_cast<double2 *>(w + o_st), err, s);
@@ -451,6 +496,9 @@ gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms) {
     GPP_CUDA_TRY(cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost), "read fault word");
     if (h) {
         GPP_CUDA_TRY(cudaMemset(err, 0, sizeof(int)), "clear fault word");
+        if (h & kErrPipelineTimeout)
+            return fail(GPP_ERR_DEVICE_TIMEOUT,
+                        "a kernel's shared-memory pipeline wait gave up; results are invalid");
         return fail(GPP_ERR_BAD_INDEX, "device saw %s%s",
                     (h & kErrBadIgp) ? "inv_igp_index < 0 " : "",
                     (h & kErrBadIndinv) ? "indinv out of [0, ncouls)" : "");

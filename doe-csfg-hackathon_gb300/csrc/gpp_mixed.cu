@@ -122,10 +122,19 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
         : "memory");
     return ok != 0;
 }
-// Bounded wait for phase `parity` of `bar`; false after kWaitLimit polls.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-    for (int it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for phase `parity` of `bar`.  Gives up (returns false) after
+// kWaitLimit polls, or as soon as another thread of the block has raised
+// *abort, so a block never spins without end.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          volatile int *abort) {
+    for (int it = 0; it < kWaitLimit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63 && *abort) return false;
+    }
+    *abort = 1;
     return false;
 }
 __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes,
@@ -139,24 +148,28 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
 
 // Unoccupied bands, mixed precision.  A block owns RG local G' rows and
 // NWARP * RNW bands; warp w owns bands band0 + w*RNW .. +RNW-1.  The ig range
-// is processed in chunks of KC columns: thread 0 streams each chunk's row
-// planes (wtilde, Q: RG x KC x 16 B each) and band planes (aqsn: NWARP*RNW x
-// KC x 16 B) into a double-buffered shared-memory stage with 1-D bulk TMA
-// copies; every warp then reads the rows from shared memory (one copy serves
-// all warps) and its own bands, lanes on consecutive ig (conflict-free 16-byte
-// LDS).  Per-lane df sums are reduced across the warp with a fixed shuffle
-// tree in df arithmetic, converted to FP64 once, and combined by the common
-// epilogue.
-template <int RNW, int RG, int NWC, int NWARP, int KC, int GROUP>
-__global__ void __launch_bounds__(NWARP * 32)
+// is processed in chunks of KC columns through an NSTAGE-deep shared-memory
+// ring: thread 0 streams each chunk's row planes (wtilde, Q: RG x KC x 16 B
+// each) and band planes (aqsn: NWARP*RNW x KC x 16 B) into a stage with 1-D
+// bulk TMA copies that complete on the stage's "full" mbarrier; each warp
+// reads the rows (one copy serves all warps) and its own bands, lanes on
+// consecutive ig (conflict-free 16-byte LDS), then arrives on the stage's
+// "empty" mbarrier.  The producer refills a stage one chunk behind the
+// consumers, so warps run decoupled without block-wide barriers.  Per-lane df
+// sums are reduced across the warp with a fixed shuffle tree in df
+// arithmetic, converted to FP64 once, and combined by the common epilogue.
+template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int GROUP>
+__global__ void __launch_bounds__(NWARP * 32, NWC <= 3 ? 5 : 4)
 mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
                     int row_tiles, int band_tiles) {
-    constexpr int BN = NWARP * RNW;           // bands per block
-    constexpr int K = BN * RG * NWC * 2;      // doubles in the block result
-    constexpr int STAGE = (2 * RG + BN) * KC; // float4 per stage
+    constexpr int BN = NWARP * RNW;            // bands per block
+    constexpr int K = BN * RG * NWC * 2;       // doubles in the block result
+    constexpr int STAGE = (2 * RG + BN) * KC;  // float4 per stage
     static_assert(KC % 32 == 0, "chunk must be a multiple of the warp width");
+    static_assert(NSTAGE >= 2, "need at least two stages");
     extern __shared__ __align__(128) float4 stage_mem[];
-    __shared__ unsigned long long bars[2];
+    __shared__ unsigned long long full_bar[NSTAGE], empty_bar[NSTAGE];
+    __shared__ int abort_flag;
     __shared__ double S[K];
 
     const int tiles_per_group = GROUP * band_tiles;
@@ -171,14 +184,15 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
     const int nc = p.nc;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nchunks = (nc + KC - 1) / KC;
+    volatile int *abort = &abort_flag;
 
-    // Producer: copy chunk c into stage (c & 1).
+    // Producer: copy chunk c into stage c % NSTAGE.
     auto issue = [&](int c) {
         const int k0 = c * KC;
         const int cnt = min(KC, nc - k0);
         const unsigned bytes = (unsigned)cnt * 16u;
-        float4 *st = stage_mem + (c & 1) * STAGE;
-        unsigned long long *bar = &bars[c & 1];
+        float4 *st = stage_mem + (c % NSTAGE) * STAGE;
+        unsigned long long *bar = &full_bar[c % NSTAGE];
         mbar_expect_tx(bar, bytes * (2 * RG + BN));
 #pragma unroll
         for (int g = 0; g < RG; ++g) {
@@ -194,15 +208,17 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
     };
 
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        abort_flag = 0;
+        for (int i = 0; i < NSTAGE; ++i) {
+            mbar_init(&full_bar[i], 1);
+            mbar_init(&empty_bar[i], NWARP);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        issue(0);
-        if (nchunks > 1) issue(1);
-    }
+    int issued = 0;  // chunks issued so far (thread 0 only)
+    if (threadIdx.x == 0)
+        for (; issued < NSTAGE - 1 && issued < nchunks; ++issued) issue(issued);
 
     df wx[RNW][NWC];
     float pole_thr[RNW][NWC];
@@ -227,14 +243,27 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
                 acc[n][g][w][1] = {0.f, 0.f};
             }
 
-    bool timed_out = false;
-    unsigned parity[2] = {0u, 0u};
+    int c_stop = nchunks;  // first chunk this thread did not consume
     for (int c = 0; c < nchunks; ++c) {
-        const int sidx = c & 1;
-        const bool ok = mbar_wait(&bars[sidx], parity[sidx]);
-        parity[sidx] ^= 1u;
-        if (__syncthreads_or(!ok)) {
-            timed_out = true;
+        // Refill: chunk c + NSTAGE - 1 goes into the stage consumed at c - 1.
+        // The whole of warp 0 waits for its lane 0 here, so the warp stays
+        // converged for the compute below.
+        if (threadIdx.x == 0 && issued < nchunks && !*abort) {
+            const int sp = issued % NSTAGE;
+            if (issued >= NSTAGE) {
+                const unsigned par = (unsigned)((issued / NSTAGE - 1) & 1);
+                if (mbar_wait(&empty_bar[sp], par, abort)) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(issued++);
+                }
+            } else {
+                issue(issued++);
+            }
+        }
+        if (warp == 0) __syncwarp();
+        const int sidx = c % NSTAGE;
+        if (!mbar_wait(&full_bar[sidx], (unsigned)((c / NSTAGE) & 1), abort)) {
+            c_stop = c;
             break;
         }
         const float4 *st = stage_mem + sidx * STAGE;
@@ -247,10 +276,10 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
             for (int g = 0; g < RG; ++g) {
                 const float4 wv = st[g * KC + il];
                 const float4 qv = st[(RG + g) * KC + il];
-                wtr[g] = {wv.x, wv.y};
-                wti[g] = {wv.z, wv.w};
-                qr[g] = {qv.x, qv.y};
-                qi[g] = {qv.z, qv.w};
+                wtr[g] = df{wv.x, wv.y};
+                wti[g] = df{wv.z, wv.w};
+                qr[g] = df{qv.x, qv.y};
+                qi[g] = df{qv.z, qv.w};
                 wti2[g] = df_sqr(wti[g]);
             }
 #pragma unroll
@@ -285,18 +314,20 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
                 }
             }
         }
-        __syncthreads();  // every warp is done with this stage
-        if (threadIdx.x == 0 && c + 2 < nchunks) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(c + 2);
-        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty_bar[sidx]);
     }
 
-    if (timed_out) {
+    if (__syncthreads_or(*abort)) {
         if (threadIdx.x == 0) {
             atomicOr(part.err, kErrPipelineTimeout);
-            // Let copies still in flight land before the block retires.
-            for (int b = 0; b < 2; ++b) mbar_wait(&bars[b], parity[b]);
+            // Let the copies still in flight land before the block retires.
+            for (int j = c_stop; j < issued; ++j) {
+                int spin = 0;
+                while (!mbar_try_wait(&full_bar[j % NSTAGE], (unsigned)((j / NSTAGE) & 1)) &&
+                       ++spin < kWaitLimit) {
+                }
+            }
         }
         return;
     }
@@ -328,15 +359,16 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
 
 constexpr int kGroup = 16;
 constexpr int kWarps = 4;
-constexpr int kChunk = 128;
+constexpr int kChunk = 64;
+constexpr int kStages = 4;
 
 template <int RNW, int RG, int NWC>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
                            int b1, cudaStream_t st) {
     constexpr int BN = kWarps * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
-    const size_t smem = sizeof(float4) * 2 * (2 * RG + BN) * kChunk;
-    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, kChunk, kGroup>;
+    const size_t smem = sizeof(float4) * kStages * (2 * RG + BN) * kChunk;
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, kChunk, kStages, kGroup>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);

@@ -17,6 +17,7 @@ GPP_ERR_OUT_OF_MEMORY = 3
 GPP_ERR_UNSUPPORTED = 4
 GPP_ERR_BAD_INDEX = 5
 GPP_ERR_NOT_READY = 6
+GPP_ERR_DEVICE_TIMEOUT = 7
 
 PRECISION = {"fp64": 0, "mixed": 1}
 SEMANTICS = {"complex_seq": 0, "kerseq": 1}

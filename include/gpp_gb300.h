@@ -48,7 +48,8 @@ typedef enum gpp_status {
     GPP_ERR_OUT_OF_MEMORY = 3,    /* workspace or staging allocation failed */
     GPP_ERR_UNSUPPORTED = 4,      /* option not available for these sizes */
     GPP_ERR_BAD_INDEX = 5,        /* device saw inv_igp_index < 0 or indinv out of range */
-    GPP_ERR_NOT_READY = 6         /* gpp_wait timed out; the work is still running */
+    GPP_ERR_NOT_READY = 6,        /* gpp_wait timed out; the work is still running */
+    GPP_ERR_DEVICE_TIMEOUT = 7    /* a kernel's bounded wait gave up; that call's results are invalid */
 } gpp_status;
 
 typedef enum gpp_precision {
@@ -154,8 +155,9 @@ gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_str
 
 /* Waits for `stream` (at most timeout_ms; < 0 waits forever) and reports
  * device-side faults of earlier gpp_sigma calls on this device: returns
- * GPP_ERR_BAD_INDEX once if a kernel saw an invalid index (and clears the
- * flag), GPP_ERR_NOT_READY on timeout. */
+ * GPP_ERR_DEVICE_TIMEOUT or GPP_ERR_BAD_INDEX once if a kernel gave up a
+ * bounded wait or saw an invalid index (and clears the flag),
+ * GPP_ERR_NOT_READY if the stream is still busy after timeout_ms. */
 gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms);
 
 /* Host-memory convenience path (end-to-end): every array pointer in
