@@ -9,6 +9,7 @@
 #include <thread>
 #include <vector>
 #include <chrono>
+#include <cstdlib>
 
 #include "gpp_gb300.h"
 #include "gpp_kernels.h"
@@ -149,6 +150,49 @@ struct OutSpec {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Pipeline variant of the mixed kernel per (device, frequency chunk): chosen
+// by gpp_autotune or gpp_set_variant, else the compiled-in default.  A
+// thread-local override lets the autotuner time each variant.
+std::mutex g_tune_mutex;
+int g_tuned[256][9];  // [device][nwc 1..8]; 0 = unset, else variant + 1
+bool g_tune_loaded = false;
+thread_local int t_force_variant = -1;
+
+int nwc_of(int nw) { return nw <= 4 ? nw : 8; }
+
+void tune_cache_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = getenv("GPP_TUNE_CACHE");
+    if (!path) return;
+    FILE *f = fopen(path, "r");
+    if (!f) return;
+    int dev, nwc, v;
+    while (fscanf(f, "%d %d %d", &dev, &nwc, &v) == 3)
+        if (dev >= 0 && dev < 256 && nwc >= 1 && nwc <= 8 && v >= 0 && v < mixed_variant_count())
+            g_tuned[dev][nwc] = v + 1;
+    fclose(f);
+}
+
+void tune_cache_save_locked() {
+    const char *path = getenv("GPP_TUNE_CACHE");
+    if (!path) return;
+    FILE *f = fopen(path, "w");
+    if (!f) return;
+    for (int d = 0; d < 256; ++d)
+        for (int n = 1; n <= 8; ++n)
+            if (g_tuned[d][n]) fprintf(f, "%d %d %d\n", d, n, g_tuned[d][n] - 1);
+    fclose(f);
+}
+
+int mixed_variant_for(int dev, int nw) {
+    if (t_force_variant >= 0) return t_force_variant;
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    tune_cache_load_locked();
+    const int v = g_tuned[dev & 255][nwc_of(nw)];
+    return v ? v - 1 : mixed_default_variant();
+}
+
 // Per host thread and device: a highest-priority side stream plus fork/join
 // events.  The mixed path runs the FP64 occupied-band kernel there, beside the
 // FP32 unoccupied-band kernel: the two keep different pipes busy on the same
@@ -254,7 +298,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     if (e == cudaSuccess && has_noflag) {
         part.ach_tile0 = (int)tiles_f;
         if (t_timing && t_ev0) cudaEventRecord(t_ev0, s);
-        e = mixed ? launch_mixed_noflag(p, part, w + o_split, nb0, nb1, s)
+        e = mixed ? launch_mixed_noflag(p, part, w + o_split, nb0, nb1, s,
+                                        mixed_variant_for(dev, p.nw))
                   : launch_noflag_fp64(p, part, nb0, nb1, s);
         if (t_timing && t_ev1) {
             cudaEventRecord(t_ev1, s);
@@ -611,6 +656,90 @@ gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *out
         gpp_status st = gpp_sigma(problems + i, outs + i, stream);
         if (st != GPP_OK) return st;
     }
+    return GPP_OK;
+}
+
+int gpp_variant_count(void) { return mixed_variant_count(); }
+const char *gpp_variant_name(int variant) { return mixed_variant_name(variant); }
+
+gpp_status gpp_set_variant(int nw, int variant) {
+    if (nw <= 0 || variant < -1 || variant >= mixed_variant_count())
+        return fail(GPP_ERR_INVALID_ARGUMENT, "bad nw or variant");
+    int dev = 0;
+    GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    tune_cache_load_locked();
+    g_tuned[dev & 255][nwc_of(nw)] = variant + 1;  // -1 clears back to the default
+    return GPP_OK;
+}
+
+gpp_status gpp_tuned_variant(int nw, int *variant) {
+    if (nw <= 0 || !variant) return fail(GPP_ERR_INVALID_ARGUMENT, "bad nw or NULL output");
+    int dev = 0;
+    GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    *variant = mixed_variant_for(dev, nw);
+    return GPP_OK;
+}
+
+gpp_status gpp_autotune(const gpp_problem *problem, int max_bands, gpp_stream_t stream,
+                        int *best) {
+    gpp_status st = validate(problem);
+    if (st != GPP_OK) return st;
+    if (problem->precision != GPP_PRECISION_MIXED)
+        return fail(GPP_ERR_UNSUPPORTED, "the autotuner selects mixed-precision variants");
+    Problem p = to_problem(*problem);
+    // Time the unoccupied bands only (the variants differ there), at most
+    // max_bands of them.
+    const int unocc = p.nb - p.nv;
+    if (unocc <= 0 || p.ng == 0) return fail(GPP_ERR_INVALID_ARGUMENT, "no unoccupied bands to time");
+    const int nbt = (max_bands > 0 && max_bands < unocc) ? max_bands : unocc;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int dev = 0;
+    GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+    double2 *out = nullptr;
+    GPP_CUDA_TRY(cudaMallocAsync(&out, sizeof(double2) * 2 * (size_t)p.nw, s), "cudaMallocAsync");
+    OutSpec o;
+    o.ach = out;
+    o.asx = out + p.nw;
+    cudaEvent_t e0, e1;
+    GPP_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+    GPP_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+    float best_ms = 0.f;
+    int best_v = -1;
+    const bool timing = t_timing;
+    t_timing = false;
+    for (int v = 0; v < mixed_variant_count() && st == GPP_OK; ++v) {
+        t_force_variant = v;
+        float vbest = 0.f;
+        for (int rep = 0; rep < 3 && st == GPP_OK; ++rep) {
+            cudaEventRecord(e0, s);
+            st = run_sigma(p, p.nv, p.nv + nbt, GPP_PRECISION_MIXED, o, true, s);
+            cudaEventRecord(e1, s);
+            if (st != GPP_OK) break;
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) { st = cuda_fail(e, "autotune"); break; }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && (vbest == 0.f || ms < vbest)) vbest = ms;  // rep 0 warms up
+        }
+        if (st == GPP_OK && (best_v < 0 || vbest < best_ms)) {
+            best_ms = vbest;
+            best_v = v;
+        }
+    }
+    t_force_variant = -1;
+    t_timing = timing;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(out, s);
+    if (st != GPP_OK) return st;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        tune_cache_load_locked();
+        g_tuned[dev & 255][nwc_of(p.nw)] = best_v + 1;
+        tune_cache_save_locked();
+    }
+    if (best) *best = best_v;
     return GPP_OK;
 }
 

@@ -48,7 +48,11 @@ cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 size_t mixed_split_bytes(const Problem &p);
 TileShape mixed_noflag_shape(const Problem &p);
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws,
-                                int band_begin, int band_end, cudaStream_t s);
+                                int band_begin, int band_end, cudaStream_t s, int variant);
+// Pipeline variants of the mixed kernel, selectable per call (autotuner).
+int mixed_variant_count();
+const char *mixed_variant_name(int variant);
+int mixed_default_variant();
 
 // Per-thread launch counter (gpp_launch_count).
 void count_launch(int n = 1);

@@ -146,6 +146,61 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
         : "memory");
 }
 
+// The df arithmetic of one ig column for one warp: RNW bands x RG rows x NWC
+// frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into acc.  Terms
+// within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs.
+template <int RNW, int RG, int NWC, int KC>
+__device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
+                                             const float4 *sb, int il, int ig,
+                                             int row0, int bandw, int band_end, int iw0,
+                                             const df (&wx)[RNW][NWC],
+                                             const float (&pole_thr)[RNW][NWC],
+                                             df (&acc)[RNW][RG][NWC][2]) {
+    df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const float4 wv = st[g * KC + il];
+        const float4 qv = st[(RG + g) * KC + il];
+        wtr[g] = df{wv.x, wv.y};
+        wti[g] = df{wv.z, wv.w};
+        qr[g] = df{qv.x, qv.y};
+        qi[g] = df{qv.z, qv.w};
+        wti2[g] = df_sqr(wti[g]);
+    }
+#pragma unroll
+    for (int n = 0; n < RNW; ++n) {
+        const float4 av = sb[n * KC + il];
+        const df ar = {av.x, av.y}, ai = {av.z, av.w};
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            // A = aqsn * Q (frequency independent)
+            const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
+            const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
+            const df Ai_wti = df_mul(Ai, wti[g]);
+            const df Ar_wti = df_mul(Ar, wti[g]);
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
+                const df d = df_add(df_sqr(wr), wti2[g]);         // |wdiff|^2
+                df tre, tim;
+                if (d.h >= pole_thr[n][w]) {
+                    const df r = df_rcp(d);
+                    // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
+                    tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
+                    tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
+                } else {
+                    pole_term_fp64(p, min(row0 + g, p.ng - 1), min(bandw + n, band_end - 1), ig,
+                                   min(iw0 + w, p.nw - 1), tre, tim);
+                }
+                acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
+                acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
+            }
+        }
+    }
+}
+
+enum : int { kSyncBlock = 0, kSyncRing = 1 };
+
 // Unoccupied bands, mixed precision.  A block owns RG local G' rows and
 // NWARP * RNW bands; warp w owns bands band0 + w*RNW .. +RNW-1.  The ig range
 // is processed in chunks of KC columns through an NSTAGE-deep shared-memory
@@ -153,13 +208,18 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
 // each) and band planes (aqsn: NWARP*RNW x KC x 16 B) into a stage with 1-D
 // bulk TMA copies that complete on the stage's "full" mbarrier; each warp
 // reads the rows (one copy serves all warps) and its own bands, lanes on
-// consecutive ig (conflict-free 16-byte LDS), then arrives on the stage's
-// "empty" mbarrier.  The producer refills a stage one chunk behind the
-// consumers, so warps run decoupled without block-wide barriers.  Per-lane df
-// sums are reduced across the warp with a fixed shuffle tree in df
-// arithmetic, converted to FP64 once, and combined by the common epilogue.
-template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int GROUP>
-__global__ void __launch_bounds__(NWARP * 32, NWC <= 3 ? 5 : 4)
+// consecutive ig (conflict-free 16-byte LDS).  Two ways to recycle a stage:
+//  * kSyncBlock: one __syncthreads per chunk; the refill of the stage read in
+//    the previous chunk is issued right after it, NSTAGE-1 chunks ahead;
+//  * kSyncRing: each warp arrives on the stage's "empty" mbarrier, and the
+//    producer refills a stage one chunk behind the consumers, so warps run
+//    decoupled without block-wide barriers.
+// Per-lane df sums are reduced across the warp with a fixed shuffle tree in
+// df arithmetic, converted to FP64 once, and combined by the common epilogue.
+// Every wait is bounded (kWaitLimit polls, or an abort raised by another
+// thread of the block); a block that gives up records kErrPipelineTimeout.
+template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int SYNC, int GROUP>
+__global__ void __launch_bounds__(NWARP * 32)
 mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
                     int row_tiles, int band_tiles) {
     constexpr int BN = NWARP * RNW;            // bands per block
@@ -183,6 +243,7 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
     const int iw0 = blockIdx.y * NWC;
     const int nc = p.nc;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bandw = band0 + warp * RNW;
     const int nchunks = (nc + KC - 1) / KC;
     volatile int *abort = &abort_flag;
 
@@ -224,7 +285,7 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
     float pole_thr[RNW][NWC];
 #pragma unroll
     for (int n = 0; n < RNW; ++n) {
-        const int b = min(band0 + warp * RNW + n, band_end - 1);
+        const int b = min(bandw + n, band_end - 1);
 #pragma unroll
         for (int w = 0; w < NWC; ++w) {
             const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
@@ -243,79 +304,49 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
                 acc[n][g][w][1] = {0.f, 0.f};
             }
 
-    int c_stop = nchunks;  // first chunk this thread did not consume
+    int c_stop = nchunks;  // first chunk thread 0 did not consume
     for (int c = 0; c < nchunks; ++c) {
-        // Refill: chunk c + NSTAGE - 1 goes into the stage consumed at c - 1.
-        // The whole of warp 0 waits for its lane 0 here, so the warp stays
-        // converged for the compute below.
+        // Refill the stage that chunk c - 1 used with chunk c + NSTAGE - 1.
         if (threadIdx.x == 0 && issued < nchunks && !*abort) {
-            const int sp = issued % NSTAGE;
-            if (issued >= NSTAGE) {
+            if (SYNC == kSyncBlock || issued < NSTAGE) {
+                if (issued >= NSTAGE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(issued++);
+            } else {
+                const int sp = issued % NSTAGE;
                 const unsigned par = (unsigned)((issued / NSTAGE - 1) & 1);
                 if (mbar_wait(&empty_bar[sp], par, abort)) {
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     issue(issued++);
                 }
-            } else {
-                issue(issued++);
             }
         }
-        if (warp == 0) __syncwarp();
+        if (SYNC == kSyncRing && warp == 0) __syncwarp();  // warp 0 waits for its producer lane
         const int sidx = c % NSTAGE;
-        if (!mbar_wait(&full_bar[sidx], (unsigned)((c / NSTAGE) & 1), abort)) {
-            c_stop = c;
-            break;
-        }
-        const float4 *st = stage_mem + sidx * STAGE;
-        const int k0 = c * KC;
-        const int cnt = min(KC, nc - k0);
+        const bool ok = mbar_wait(&full_bar[sidx], (unsigned)((c / NSTAGE) & 1), abort);
+        if (ok) {
+            const float4 *st = stage_mem + sidx * STAGE;      // row planes
+            const float4 *sb = st + (2 * RG + warp * RNW) * KC;  // this warp's bands
+            const int k0 = c * KC;
+            const int cnt = min(KC, nc - k0);
 #pragma unroll 1
-        for (int il = lane; il < cnt; il += 32) {
-            df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
-#pragma unroll
-            for (int g = 0; g < RG; ++g) {
-                const float4 wv = st[g * KC + il];
-                const float4 qv = st[(RG + g) * KC + il];
-                wtr[g] = df{wv.x, wv.y};
-                wti[g] = df{wv.z, wv.w};
-                qr[g] = df{qv.x, qv.y};
-                qi[g] = df{qv.z, qv.w};
-                wti2[g] = df_sqr(wti[g]);
-            }
-#pragma unroll
-            for (int n = 0; n < RNW; ++n) {
-                const float4 av = st[(2 * RG + warp * RNW + n) * KC + il];
-                const df ar = {av.x, av.y}, ai = {av.z, av.w};
-#pragma unroll
-                for (int g = 0; g < RG; ++g) {
-                    // A = aqsn * Q (frequency independent)
-                    const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
-                    const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
-                    const df Ai_wti = df_mul(Ai, wti[g]);
-                    const df Ar_wti = df_mul(Ar, wti[g]);
-#pragma unroll
-                    for (int w = 0; w < NWC; ++w) {
-                        const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
-                        const df d = df_add(df_sqr(wr), wti2[g]);         // |wdiff|^2
-                        df tre, tim;
-                        if (d.h >= pole_thr[n][w]) {
-                            const df r = df_rcp(d);
-                            // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
-                            tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
-                            tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
-                        } else {
-                            pole_term_fp64(p, min(row0 + g, p.ng - 1),
-                                           min(band0 + warp * RNW + n, band_end - 1), k0 + il,
-                                           min(iw0 + w, p.nw - 1), tre, tim);
-                        }
-                        acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
-                        acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
-                    }
-                }
-            }
+            for (int il = lane; il < cnt; il += 32)
+                mixed_column<RNW, RG, NWC, KC>(p, st, sb, il, k0 + il, row0, bandw, band_end,
+                                               iw0, wx, pole_thr, acc);
         }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty_bar[sidx]);
+        if (SYNC == kSyncBlock) {
+            __syncthreads();  // every warp is done with stage sidx
+            if (*abort) {
+                c_stop = c;
+                break;
+            }
+        } else {
+            if (!ok) {
+                c_stop = c;
+                break;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty_bar[sidx]);
+        }
     }
 
     if (__syncthreads_or(*abort)) {
@@ -359,16 +390,27 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
 
 constexpr int kGroup = 16;
 constexpr int kWarps = 4;
-constexpr int kChunk = 64;
-constexpr int kStages = 4;
 
-template <int RNW, int RG, int NWC>
+// Compiled pipeline variants of the mixed kernel (the autotuner picks one).
+struct MixedVariant {
+    int kc, stages, sync;
+    const char *name;
+};
+constexpr MixedVariant kMixedVariants[] = {
+    {128, 2, kSyncBlock, "block-sync, 2 x 128 columns"},
+    {128, 3, kSyncBlock, "block-sync, 3 x 128 columns"},
+    {128, 2, kSyncRing, "mbarrier ring, 2 x 128 columns"},
+    {64, 4, kSyncRing, "mbarrier ring, 4 x 64 columns"},
+};
+constexpr int kNumMixedVariants = sizeof(kMixedVariants) / sizeof(kMixedVariants[0]);
+
+template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
                            int b1, cudaStream_t st) {
     constexpr int BN = kWarps * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
-    const size_t smem = sizeof(float4) * kStages * (2 * RG + BN) * kChunk;
-    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, kChunk, kStages, kGroup>;
+    const size_t smem = sizeof(float4) * NSTAGE * (2 * RG + BN) * KC;
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
@@ -378,6 +420,17 @@ cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPl
     kern<<<grid, kWarps * 32, smem, st>>>(p, part, s, b0, b1, row_tiles, band_tiles);
     count_launch();
     return cudaGetLastError();
+}
+
+template <int RNW, int RG, int NWC>
+cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
+                                 const SplitPlanes &s, int b0, int b1, cudaStream_t st) {
+    switch (v) {
+        case 0: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, st);
+        case 2: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, st);
+        case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, st);
+        default: return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
+    }
 }
 
 }  // namespace
@@ -393,13 +446,19 @@ TileShape mixed_noflag_shape(const Problem &p) {
     return TileShape{kWarps, mixed_rg(nwc), nwc, kWarps * 32};
 }
 
+int mixed_variant_count() { return kNumMixedVariants; }
+const char *mixed_variant_name(int v) {
+    return (v >= 0 && v < kNumMixedVariants) ? kMixedVariants[v].name : "default";
+}
+int mixed_default_variant() { return 1; }
+
 size_t mixed_split_bytes(const Problem &p) {
     return sizeof(float4) * ((size_t)2 * p.ng * p.nc + (size_t)p.nb * p.nc) +
            sizeof(float2) * (size_t)p.nb * p.nw;
 }
 
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws, int b0,
-                                int b1, cudaStream_t st) {
+                                int b1, cudaStream_t st, int variant) {
     if (b1 <= b0 || p.ng == 0) return cudaSuccess;
     const SplitPlanes s = planes(p, split_ws);
     int dev = 0, sms = 0;
@@ -412,11 +471,11 @@ cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *sp
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_mixed_t<1, 2, 1>(p, part, s, b0, b1, st);
-        case 2: return launch_mixed_t<1, 2, 2>(p, part, s, b0, b1, st);
-        case 3: return launch_mixed_t<1, 2, 3>(p, part, s, b0, b1, st);
-        case 4: return launch_mixed_t<1, 2, 4>(p, part, s, b0, b1, st);
-        default: return launch_mixed_t<1, 1, 8>(p, part, s, b0, b1, st);
+        case 1: return launch_mixed_t<1, 2, 1, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
+        case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
+        case 3: return launch_mixed_variant<1, 2, 3>(variant, p, part, s, b0, b1, st);
+        case 4: return launch_mixed_t<1, 2, 4, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
+        default: return launch_mixed_variant<1, 1, 8>(variant, p, part, s, b0, b1, st);
     }
 }
 

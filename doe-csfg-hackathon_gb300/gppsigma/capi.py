@@ -53,6 +53,11 @@ _SIGS = {
     "gpp_sigma_host": (_i, [_vp, C.POINTER(GppProblem), C.POINTER(GppOutputs)]),
     "gpp_sigma_batched": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _i, _vp]),
     "gpp_sigma_static_scratch": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _vp]),
+    "gpp_autotune": (_i, [C.POINTER(GppProblem), _i, _vp, C.POINTER(_i)]),
+    "gpp_set_variant": (_i, [_i, _i]),
+    "gpp_tuned_variant": (_i, [_i, C.POINTER(_i)]),
+    "gpp_variant_count": (_i, []),
+    "gpp_variant_name": (C.c_char_p, [_i]),
     "gpp_last_error_message": (C.c_char_p, []),
     "gpp_launch_count": (C.c_ulonglong, []),
     "gpp_reset_launch_count": (None, []),

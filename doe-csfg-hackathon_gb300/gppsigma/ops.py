@@ -204,6 +204,26 @@ def sigma(d: DeviceInputs, precision: str = "fp64", semantics: str = "complex_se
     return out
 
 
+def autotune(d: DeviceInputs, max_bands: int = 64, semantics: str = "complex_seq") -> int:
+    """Time the mixed kernel's pipeline variants on `d` (first `max_bands`
+    unoccupied bands) and keep the fastest for this frequency chunk."""
+    lib = capi.load()
+    p = problem_struct(d, "mixed", semantics, 1.0)
+    best = C.c_int(-1)
+    capi.check(lib.gpp_autotune(C.byref(p), max_bands, _stream(), C.byref(best)), "gpp_autotune")
+    return best.value
+
+
+def set_variant(nw: int, variant: int) -> None:
+    """Force a mixed-kernel pipeline variant for `nw` frequencies (-1: default)."""
+    capi.check(capi.load().gpp_set_variant(nw, variant), "gpp_set_variant")
+
+
+def variant_names() -> list[str]:
+    lib = capi.load()
+    return [lib.gpp_variant_name(i).decode() for i in range(lib.gpp_variant_count())]
+
+
 def wait(timeout_ms: int = -1) -> None:
     """Synchronise the current stream and raise on device-side index faults."""
     capi.check(capi.load().gpp_wait(_stream(), timeout_ms), "gpp_wait")

@@ -193,6 +193,23 @@ gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *out
                              gpp_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Autotuner for the mixed-precision unoccupied-band kernel.  It is compiled
+ * in a few pipeline variants (shared-memory chunk width, stage count, block
+ * barrier vs mbarrier ring).  gpp_autotune times every variant on `problem`
+ * (its first max_bands unoccupied bands; 0 = all) on `stream`, keeps the
+ * fastest for problems with the same frequency chunk on the current device,
+ * and writes the choice to the file named by the GPP_TUNE_CACHE environment
+ * variable, if set (read back on first use).  gpp_set_variant overrides the
+ * choice (-1 restores the default); gpp_tuned_variant reports it.
+ * ------------------------------------------------------------------------ */
+gpp_status gpp_autotune(const gpp_problem *problem, int max_bands, gpp_stream_t stream,
+                        int *best_variant);
+gpp_status gpp_set_variant(int nw, int variant);
+gpp_status gpp_tuned_variant(int nw, int *variant);
+int gpp_variant_count(void);
+const char *gpp_variant_name(int variant);
+
+/* ------------------------------------------------------------------------
  * Introspection and measurement support.
  * ------------------------------------------------------------------------ */
 

@@ -79,3 +79,25 @@ def test_production_near_pole_mixed_within_1e8_of_fp64():
     ex = rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy())
     print(f"mixed vs fp64: achtemp {ea:.3e}, asxtemp {ex:.3e}")
     assert ea <= MIXED_TOL and ex <= MIXED_TOL
+
+
+def test_every_pipeline_variant_gives_the_same_bits_and_autotune_picks_one():
+    o = ops()
+    shape = W.Shape(20, 2, 3000, 40, 3, near_pole=0.01)
+    d = o.DeviceInputs.from_host(W.make_inputs(shape, 9))
+    ref = None
+    names = o.variant_names()
+    assert len(names) >= 2
+    try:
+        for v in range(len(names)):
+            o.set_variant(3, v)
+            r = o.sigma(d, "mixed")
+            o.wait()
+            got = torch.view_as_real(r.achtemp).cpu()
+            if ref is None:
+                ref = got
+            assert torch.equal(got, ref), names[v]
+        best = o.autotune(d, max_bands=8)
+        assert 0 <= best < len(names)
+    finally:
+        o.set_variant(3, -1)

@@ -1,0 +1,99 @@
+"""Host-side multi-rank logic with world_size 2 over gloo on the CPU: the
+slowest-rank timing, whole-job rate, rank-ordered partial sums of a sharded
+state (checked against the oracle), and a failing rank surfacing as an error
+on its peer instead of a hang."""
+import datetime
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+import torch.multiprocessing as mp
+
+from conftest import PKG_ROOT, REPO
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, mode, out):
+    sys.path.insert(0, PKG_ROOT)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import torch.distributed as dist
+    from gppsigma import dist as gd, workload as W
+    import oracle_py
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world, timeout=datetime.timedelta(seconds=20))
+    try:
+        if mode == "timing":
+            ms = 10.0 * (rank + 1)
+            out[rank] = (gd.max_over_ranks(ms, dist), gd.job_rate(1e9, ms * 1e-3, dist))
+        elif mode == "shard":
+            # One state, bands split across ranks; partial sums added on rank 0.
+            inp = W.make_inputs(W.Shape(8, 2, 300, 9, 3), 5)
+            a, b = (0, 4) if rank == 0 else (4, 8)
+            part = oracle_py.run(inp, band_begin=a, band_end=b)["achtemp"]
+            total = gd.sum_in_rank_order(part, dist)
+            if rank == 0:
+                out[0] = total
+        elif mode == "rank_fails":
+            if rank == 1:
+                raise RuntimeError("rank 1 fails before the collective")
+            try:
+                gd.max_over_ranks(1.0, dist)
+                out[0] = "no error"
+            except Exception as e:  # the peer's failure must surface, not hang
+                out[0] = type(e).__name__
+    finally:
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+def _run(mode):
+    mgr = mp.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    ctx = mp.get_context("spawn")
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, mode, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        if p.is_alive():
+            p.kill()
+            pytest.fail("worker did not finish")
+    return dict(out), [p.exitcode for p in procs]
+
+
+def test_slowest_rank_sets_the_job_time():
+    out, codes = _run("timing")
+    assert codes == [0, 0]
+    for r in (0, 1):
+        slowest, rate = out[r]
+        assert slowest == 20.0
+        assert rate == pytest.approx(2 * 1e9 / 0.020)
+
+
+def test_sharded_state_partials_add_up_in_rank_order():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    from gppsigma import workload as W
+    out, codes = _run("shard")
+    assert codes == [0, 0]
+    want = oracle_py.run(W.make_inputs(W.Shape(8, 2, 300, 9, 3), 5))["achtemp"]
+    np.testing.assert_allclose(out[0], want, rtol=1e-12)
+
+
+def test_failing_rank_surfaces_on_its_peer():
+    out, codes = _run("rank_fails")
+    assert codes[1] != 0
+    assert out[0] != "no error"
