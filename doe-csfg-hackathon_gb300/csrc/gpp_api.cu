@@ -205,6 +205,19 @@ struct SideStream {
 };
 thread_local SideStream t_side;
 
+// Whether the mixed path runs the occupied-band kernel concurrently on the
+// side stream (GPP_OVERLAP_OCCUPIED=1) or before the unoccupied-band kernel
+// on the caller's stream (default).  Measured on GB300 at the production
+// shape, the concurrent form was slower: the FP64 blocks take register and
+// warp slots the issue-bound FP32 kernel needs.
+bool overlap_occupied() {
+    static const bool on = [] {
+        const char *v = getenv("GPP_OVERLAP_OCCUPIED");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
 gpp_status side_stream(int dev, SideStream **out) {
     if (t_side.dev != dev) {
         int lo = 0, hi = 0;
@@ -282,7 +295,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         e = cudaMemsetAsync(part.n1, 0, sizeof(double2) * (size_t)(n1_seg * p.nb), s);
     }
     SideStream *side = nullptr;
-    const bool overlap = mixed && has_flag;
+    const bool overlap = mixed && has_flag && overlap_occupied();
     if (overlap) {
         st = side_stream(dev, &side);
         if (st != GPP_OK) {
