@@ -353,11 +353,21 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
 }
 
 }  // namespace
+
+int tuned_mixed_variant(int dev, int nw) { return mixed_variant_for(dev, nw); }
+
 }  // namespace gpp
 
 using namespace gpp;
 
 extern "C" {
+
+// The current device's fault word (used by the batch planner), or NULL.
+int *gpp_internal_fault_word(void) {
+    int dev = 0;
+    int *err = nullptr;
+    return device_setup(&dev, &err) == GPP_OK ? err : nullptr;
+}
 
 const char *gpp_last_error_message(void) { return t_err.c_str(); }
 unsigned long long gpp_launch_count(void) { return t_launches; }
@@ -658,17 +668,6 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     memcpy(out->asxtemp, tmp.data() + nw, 16 * nw);
     if (out->achstemp) out->achstemp[0] = tmp[2 * nw];
     if (out->acht_n1_loc) memcpy(out->acht_n1_loc, tmp.data() + 2 * nw + 1, 16 * nb);
-    return GPP_OK;
-}
-
-gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *outs, int nstates,
-                             gpp_stream_t stream) {
-    if (nstates < 0 || (nstates > 0 && (!problems || !outs)))
-        return fail(GPP_ERR_INVALID_ARGUMENT, "bad batch");
-    for (int i = 0; i < nstates; ++i) {
-        gpp_status st = gpp_sigma(problems + i, outs + i, stream);
-        if (st != GPP_OK) return st;
-    }
     return GPP_OK;
 }
 

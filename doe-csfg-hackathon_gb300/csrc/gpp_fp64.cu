@@ -1,32 +1,15 @@
 // gpp_fp64.cu -- FP64 CUDA-core kernels of the GPP sigma reduction for
-// sm_103a, plus the deterministic fixed-order reduction and the static term.
-//
-// Algorithm (reference: noflagOCC_solver gppComplex_seq.cpp:131-150,
-// flagOCC_solver :107-128, ssxt_scht_solver :16-63, driver :335-383).
-// The unoccupied term is regrouped, exactly in real arithmetic, as
-//
-//   mygpvar1 aqsn (delw I_eps) = conj(aqsm[n1,igp]) * A * conj(wdiff) / |wdiff|^2
-//   A = aqsn[n1,ig] * (wtilde[igp,ig] * I_eps[igp,ig]),  wdiff = wx - wtilde
-//
-// so conj(aqsm) leaves the ig sum (applied once per (n1,igp) in the block
-// epilogue) and A is shared by all frequencies.  Per term the FP64 pipe then
-// does 9 instructions: wdiff.re (DADD), |wdiff|^2 (DFMA), the reciprocal (3
-// DFMA after a seed from the multi-function unit), A*conj(wdiff) (2 DFMA with
-// the iw-independent products hoisted) and the accumulation (2 DFMA).
-//
-// Work decomposition: a block owns RG local G' rows x RN bands x NWC
-// frequencies and all ncouls columns; its threads stride over ig, so every
-// global load is a coalesced 16-byte double2 (ld.global.nc) and each loaded
-// element is reused RN*NWC (rows) or RG*NWC (bands) times from registers.
-// On GB300 the FP64 pipe retires ~2 DFMA/clk/SM, so the kernel is bound by
-// FP64 issue, not by HBM (~16 B per (n1,igp,ig) triple against ~34 FP64
-// instructions).  Partial sums: per-thread registers -> warp shuffle tree ->
-// shared-memory tree across warps -> one complex per block and frequency in
-// the workspace -> gpp_reduce_kernel sums blocks in a fixed order.  No
-// floating-point atomics anywhere: results are bit-reproducible.
+// sm_103a (one state per launch), the deterministic fixed-order reduction,
+// the static term, and the FMA throughput probe.  The tile bodies and the
+// algorithm notes live in gpp_tiles_fp64.cuh.  On GB300 the FP64 pipe
+// retires ~2 DFMA/clk/SM, so the unoccupied-band kernel is bound by FP64
+// issue, not by HBM (~16 B per (n1,igp,ig) triple against ~34 FP64
+// instructions).  No floating-point atomics anywhere: results are
+// bit-reproducible.
 #include <cstdio>
 
 #include "gpp_kernels.h"
+#include "gpp_tiles_fp64.cuh"
 
 namespace gpp {
 
@@ -38,117 +21,9 @@ noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end) {
     constexpr int K = RN * RG * NWC * 2;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-
-    const int row0 = blockIdx.x * RG;
-    const int band0 = band_begin + blockIdx.y * RN;
-    const int iw0 = blockIdx.z * NWC;
-    const int nc = p.nc;
-
-    const double2 *wrow[RG];
-    const double2 *erow[RG];
-#pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        const int r = min(row0 + g, p.ng - 1);
-        wrow[g] = p.wt + (size_t)r * nc;
-        erow[g] = p.ieps + (size_t)r * nc;
-    }
-    const double2 *nrow[RN];
-    double wx[RN][NWC];
-#pragma unroll
-    for (int n = 0; n < RN; ++n) {
-        const int b = min(band0 + n, band_end - 1);
-        nrow[n] = p.aqsn + (size_t)b * nc;
-#pragma unroll
-        for (int w = 0; w < NWC; ++w)
-            wx[n][w] = __ldg(p.wx + (size_t)b * p.wx_stride + min(iw0 + w, p.nw - 1));
-    }
-
-    double2 acc[RN][RG][NWC];
-#pragma unroll
-    for (int n = 0; n < RN; ++n)
-#pragma unroll
-        for (int g = 0; g < RG; ++g)
-#pragma unroll
-            for (int w = 0; w < NWC; ++w) acc[n][g][w] = make_double2(0.0, 0.0);
-
-    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
-        double2 Q[RG];
-        double wtr[RG], wti[RG], wti2[RG];
-#pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            const double2 wt = __ldg(wrow[g] + ig);
-            const double2 ie = __ldg(erow[g] + ig);
-            Q[g] = cmul(wt, ie);
-            wtr[g] = wt.x;
-            wti[g] = wt.y;
-            wti2[g] = wt.y * wt.y;
-        }
-#pragma unroll
-        for (int n = 0; n < RN; ++n) {
-            const double2 a = __ldg(nrow[n] + ig);
-#pragma unroll
-            for (int g = 0; g < RG; ++g) {
-                const double2 A = cmul(a, Q[g]);
-                const double ayw = A.y * wti[g];
-                const double axw = A.x * wti[g];
-#pragma unroll
-                for (int w = 0; w < NWC; ++w) {
-                    const double wr = wx[n][w] - wtr[g];   // Re(wdiff); Im(wdiff) = -wti
-                    const double d = fma(wr, wr, wti2[g]); // |wdiff|^2
-                    const double r = rcp_fp64(d);
-                    const double tx = fma(A.x, wr, -ayw);  // A * conj(wdiff)
-                    const double ty = fma(A.y, wr, axw);
-                    acc[n][g][w].x = fma(r, tx, acc[n][g][w].x);
-                    acc[n][g][w].y = fma(r, ty, acc[n][g][w].y);
-                }
-            }
-        }
-    }
-
-    double v[K];
-#pragma unroll
-    for (int n = 0; n < RN; ++n)
-#pragma unroll
-        for (int g = 0; g < RG; ++g)
-#pragma unroll
-            for (int w = 0; w < NWC; ++w) {
-                const int k = ((n * RG + g) * NWC + w) * 2;
-                v[k] = acc[n][g][w].x;
-                v[k + 1] = acc[n][g][w].y;
-            }
-    block_reduce<K, THREADS>(v, red, S);
-
-    noflag_epilogue<RN, RG, NWC>(p, part, S, row0, band0, band_end, iw0,
-                                 (long long)blockIdx.y * gridDim.x + blockIdx.x, blockIdx.x);
-}
-
-// One occupied-band term of ssxt_scht_solver (gppComplex_seq.cpp:16-63),
-// accumulated as aqsn*sch and aqsn*ssx (the conj(aqsm) factor of
-// matngmatmgp is applied in the epilogue).  cwr = 1/wx^2 for branch A.
-template <int SEM>
-__device__ __forceinline__ void flag_term(double wx, double cwr, double2 wt, double2 wt2,
-                                          double2 om2, double2 ie, double2 a, double2 &acc_s,
-                                          double2 &acc_x) {
-    const double2 wd = make_double2(wx - wt.x, -wt.y);
-    const double wdr = wd.x * wd.x + wd.y * wd.y;
-    const double rden = rcp_fp64(wdr);
-    const double2 delw = cscale(cmul_conj_b(wt, wd), rden);
-    const double delwr = delw.x * delw.x + delw.y * delw.y;
-    double2 sch = make_double2(0.0, 0.0), ssx = make_double2(0.0, 0.0);
-    if (wdr > kLimitTwo && delwr < kLimitOne) {
-        sch = cmul(delw, ie);
-        ssx = cscale(om2, cwr);
-    } else if (delwr > kTo1) {
-        const double2 cden = cscale(cmul(wt2, make_double2(0.5 + delw.x, delw.y)), 4.0);
-        const double r2 = rcp_fp64(cden.x * cden.x + cden.y * cden.y);
-        ssx = cmul(cmul_conj_b(make_double2(-om2.x, -om2.y), cden), cscale(delw, r2));
-    }
-    // |ssx| > sexcut |I_eps| compared on squares (sexcut^2 = 16 is exact).
-    if (SEM == kSemComplexSeq && wx < 0.0 &&
-        ssx.x * ssx.x + ssx.y * ssx.y > 16.0 * (ie.x * ie.x + ie.y * ie.y))
-        ssx = make_double2(0.0, 0.0);
-    acc_s = cadd(acc_s, cmul(a, sch));
-    acc_x = cadd(acc_x, cmul(a, ssx));
+    noflag_fp64_tile<RN, RG, NWC, THREADS>(p, part, band_begin, band_end, blockIdx.x, blockIdx.y,
+                                           blockIdx.z, (long long)blockIdx.y * gridDim.x + blockIdx.x,
+                                           red, S);
 }
 
 template <int RG, int NWC, int THREADS, int SEM>
@@ -156,93 +31,8 @@ __global__ void __launch_bounds__(THREADS) flag_fp64_kernel(Problem p, Partials 
     constexpr int K = RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-
-    const int row0 = blockIdx.x * RG;
-    const int band = blockIdx.y;  // one occupied band per block row
-    const int iw0 = blockIdx.z * NWC;
-    const int nc = p.nc;
-
-    const double2 *wrow[RG];
-    const double2 *erow[RG];
-#pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        const int r = min(row0 + g, p.ng - 1);
-        wrow[g] = p.wt + (size_t)r * nc;
-        erow[g] = p.ieps + (size_t)r * nc;
-    }
-    const double2 *nrow = p.aqsn + (size_t)band * nc;
-    double wx[NWC], cwr[NWC];
-#pragma unroll
-    for (int w = 0; w < NWC; ++w) {
-        wx[w] = __ldg(p.wx + (size_t)band * p.wx_stride + min(iw0 + w, p.nw - 1));
-        const double c = wx[w] * wx[w];
-        cwr[w] = c / (c * c);  // wx^2 / pow(wx^2, 2), once per (band, iw)
-    }
-
-    double2 acc_s[RG][NWC], acc_x[RG][NWC];
-#pragma unroll
-    for (int g = 0; g < RG; ++g)
-#pragma unroll
-        for (int w = 0; w < NWC; ++w) {
-            acc_s[g][w] = make_double2(0.0, 0.0);
-            acc_x[g][w] = make_double2(0.0, 0.0);
-        }
-
-    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
-        const double2 a = __ldg(nrow + ig);
-#pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            const double2 wt = __ldg(wrow[g] + ig);
-            const double2 ie = __ldg(erow[g] + ig);
-            const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
-            const double2 om2 = cmul(wt2, ie);
-#pragma unroll
-            for (int w = 0; w < NWC; ++w)
-                flag_term<SEM>(wx[w], cwr[w], wt, wt2, om2, ie, a, acc_s[g][w], acc_x[g][w]);
-        }
-    }
-
-    double v[K];
-#pragma unroll
-    for (int g = 0; g < RG; ++g)
-#pragma unroll
-        for (int w = 0; w < NWC; ++w) {
-            const int k = (g * NWC + w) * 4;
-            v[k] = acc_s[g][w].x;
-            v[k + 1] = acc_s[g][w].y;
-            v[k + 2] = acc_x[g][w].x;
-            v[k + 3] = acc_x[g][w].y;
-        }
-    block_reduce<K, THREADS>(v, red, S);
-
-    const long long tile = (long long)blockIdx.y * gridDim.x + blockIdx.x;
-    const int t = threadIdx.x;
-    // t < NWC: achtemp partial; NWC <= t < 2 NWC: asxtemp partial; t == 64: n1 column.
-    const bool do_ach = t < NWC, do_asx = t >= NWC && t < 2 * NWC, do_n1 = part.n1 && t == 64;
-    if (do_ach || do_asx || do_n1) {
-        const int w = do_ach ? t : (do_asx ? t - NWC : 2 - iw0);
-        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
-            double2 tot = make_double2(0.0, 0.0);
-#pragma unroll
-            for (int g = 0; g < RG; ++g) {
-                const int row = row0 + g;
-                if (row >= p.ng) continue;
-                const int igp = resolve_igp(p, row, part.err);
-                if (igp < 0) continue;
-                const double2 m = __ldg(p.aqsm + (size_t)band * nc + igp);
-                const int k = (g * NWC + w) * 4 + (do_asx ? 2 : 0);
-                const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
-                const double v_igp = __ldg(p.vcoul + igp);
-                tot = cadd(tot, do_asx ? cscale(s, p.occ * v_igp) : cscale(cscale(s, 0.5), v_igp));
-            }
-            if (do_ach)
-                part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + tile] = tot;
-            else if (do_asx)
-                part.asx[(long long)(iw0 + w) * part.asx_seg + tile] = tot;
-            else
-                part.n1[(long long)band * part.n1_seg + blockIdx.x] = tot;
-        }
-    }
+    flag_fp64_tile<RG, NWC, THREADS, SEM>(p, part, blockIdx.x, blockIdx.y, blockIdx.z,
+                                          (long long)blockIdx.y * gridDim.x + blockIdx.x, red, S);
 }
 
 // Static term of reduce_achstemp (gppComplex_seq.cpp:66-101): one thread per

@@ -54,6 +54,23 @@ int mixed_variant_count();
 const char *mixed_variant_name(int variant);
 int mixed_default_variant();
 
+// Float-float split planes of one state (prep pass of the mixed path).
+struct SplitPlanes;
+SplitPlanes split_planes_at(const Problem &p, void *split_ws);
+cudaError_t launch_split(const Problem &p, void *split_ws, int band_begin, int band_end,
+                         cudaStream_t s);
+
+// Persistent batched launches (gpp_batched.cu): a work queue of tiles over
+// many states.  kind 0 = occupied-band tile (band_tile is the band), 1 =
+// unoccupied-band tile; `tile` is the absolute slot in the state's achtemp
+// partial segment.
+struct BatchItem {
+    int state, kind, row_tile, band_tile, iw_chunk, tile;
+};
+
+// Pipeline variant of the mixed kernel chosen for (device, nw).
+int tuned_mixed_variant(int dev, int nw);
+
 // Per-thread launch counter (gpp_launch_count).
 void count_launch(int n = 1);
 

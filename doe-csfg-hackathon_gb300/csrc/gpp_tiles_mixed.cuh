@@ -1,0 +1,334 @@
+// gpp_tiles_mixed.cuh -- the mixed-precision unoccupied-band tile of the GPP
+// sigma reduction (float-float bulk, FP64 near the plasmon pole), shared by
+// the one-state kernel (gpp_mixed.cu) and the persistent batched kernels.
+#pragma once
+
+#include "gpp_df.cuh"
+#include "gpp_internal.cuh"
+
+namespace gpp {
+
+// Split planes written by the prep kernels (all float4 = 16 bytes).
+struct SplitPlanes {
+    float4 *rowW;  // [ng][nc]: wt.re hi, lo, wt.im hi, lo
+    float4 *rowQ;  // [ng][nc]: (wt*I_eps).re hi, lo, .im hi, lo
+    float4 *band;  // [nb][nc]: aqsn.re hi, lo, .im hi, lo
+    float2 *wx;    // [nb][nw]: wx hi, lo
+};
+
+// The full term in FP64 from the original inputs, for |wdiff| < 1e-3 |wx|.
+static __device__ __noinline__ void pole_term_fp64(const Problem &p, int row, int band, int ig, int iw,
+                                            df &re, df &im) {
+    const double2 wt = __ldg(p.wt + (size_t)row * p.nc + ig);
+    const double2 ie = __ldg(p.ieps + (size_t)row * p.nc + ig);
+    const double2 a = __ldg(p.aqsn + (size_t)band * p.nc + ig);
+    const double wx = __ldg(p.wx + (size_t)band * p.wx_stride + iw);
+    const double2 A = cmul(a, cmul(wt, ie));
+    const double wr = wx - wt.x;
+    const double r = 1.0 / (wr * wr + wt.y * wt.y);
+    const double tx = (A.x * wr - A.y * wt.y) * r;
+    const double ty = (A.y * wr + A.x * wt.y) * r;
+    re = split(tx);
+    im = split(ty);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory pipeline primitives: 1-D bulk TMA copies (cp.async.bulk)
+// completing on an mbarrier with a transaction count.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void mbar_inval(unsigned long long *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Bounded wait for phase `parity` of `bar`.  Gives up (returns false) after
+// kWaitLimit polls, or as soon as another thread of the block has raised
+// *abort, so a block never spins without end.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          volatile int *abort) {
+    for (int it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63 && *abort) return false;
+    }
+    *abort = 1;
+    return false;
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes,
+                                              unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// The df arithmetic of one ig column for one warp: RNW bands x RG rows x NWC
+// frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into acc.  Terms
+// within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs.
+template <int RNW, int RG, int NWC, int KC>
+__device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
+                                             const float4 *sb, int il, int ig,
+                                             int row0, int bandw, int band_end, int iw0,
+                                             const df (&wx)[RNW][NWC],
+                                             const float (&pole_thr)[RNW][NWC],
+                                             df (&acc)[RNW][RG][NWC][2]) {
+    df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const float4 wv = st[g * KC + il];
+        const float4 qv = st[(RG + g) * KC + il];
+        wtr[g] = df{wv.x, wv.y};
+        wti[g] = df{wv.z, wv.w};
+        qr[g] = df{qv.x, qv.y};
+        qi[g] = df{qv.z, qv.w};
+        wti2[g] = df_sqr(wti[g]);
+    }
+#pragma unroll
+    for (int n = 0; n < RNW; ++n) {
+        const float4 av = sb[n * KC + il];
+        const df ar = {av.x, av.y}, ai = {av.z, av.w};
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            // A = aqsn * Q (frequency independent)
+            const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
+            const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
+            const df Ai_wti = df_mul(Ai, wti[g]);
+            const df Ar_wti = df_mul(Ar, wti[g]);
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
+                const df d = df_add(df_sqr(wr), wti2[g]);         // |wdiff|^2
+                df tre, tim;
+                if (d.h >= pole_thr[n][w]) {
+                    const df r = df_rcp(d);
+                    // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
+                    tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
+                    tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
+                } else {
+                    pole_term_fp64(p, min(row0 + g, p.ng - 1), min(bandw + n, band_end - 1), ig,
+                                   min(iw0 + w, p.nw - 1), tre, tim);
+                }
+                acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
+                acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
+            }
+        }
+    }
+}
+
+enum : int { kSyncBlock = 0, kSyncRing = 1 };
+
+// Unoccupied bands, mixed precision.  A block owns RG local G' rows and
+// NWARP * RNW bands; warp w owns bands band0 + w*RNW .. +RNW-1.  The ig range
+// is processed in chunks of KC columns through an NSTAGE-deep shared-memory
+// ring: thread 0 streams each chunk's row planes (wtilde, Q: RG x KC x 16 B
+// each) and band planes (aqsn: NWARP*RNW x KC x 16 B) into a stage with 1-D
+// bulk TMA copies that complete on the stage's "full" mbarrier; each warp
+// reads the rows (one copy serves all warps) and its own bands, lanes on
+// consecutive ig (conflict-free 16-byte LDS).  Two ways to recycle a stage:
+//  * kSyncBlock: one __syncthreads per chunk; the refill of the stage read in
+//    the previous chunk is issued right after it, NSTAGE-1 chunks ahead;
+//  * kSyncRing: each warp arrives on the stage's "empty" mbarrier, and the
+//    producer refills a stage one chunk behind the consumers, so warps run
+//    decoupled without block-wide barriers.
+// Per-lane df sums are reduced across the warp with a fixed shuffle tree in
+// df arithmetic, converted to FP64 once, and combined by the common epilogue.
+// Every wait is bounded (kWaitLimit polls, or an abort raised by another
+// thread of the block); a block that gives up records kErrPipelineTimeout.
+// One unoccupied-band tile in mixed precision: rows row_tile*RG.., bands
+// band_begin + band_tile*BN.., frequencies iw_chunk*NWC..; `tile` indexes the
+// launch's segment of block partials.  `reinit` must be set when the block
+// ran an earlier tile with the same barriers (persistent kernels).  Returns
+// false if the tile was abandoned after a bounded wait ran out.
+template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int SYNC>
+__device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &part,
+                                           const SplitPlanes &s, int band_begin, int band_end,
+                                           int row_tile, int band_tile, int iw_chunk,
+                                           long long tile, bool reinit) {
+    constexpr int BN = NWARP * RNW;            // bands per block
+    constexpr int K = BN * RG * NWC * 2;       // doubles in the block result
+    constexpr int STAGE = (2 * RG + BN) * KC;  // float4 per stage
+    static_assert(KC % 32 == 0, "chunk must be a multiple of the warp width");
+    static_assert(NSTAGE >= 2, "need at least two stages");
+    extern __shared__ __align__(128) float4 stage_mem[];
+    __shared__ unsigned long long full_bar[NSTAGE], empty_bar[NSTAGE];
+    __shared__ int abort_flag;
+    __shared__ double S[K];
+
+    const int row0 = row_tile * RG;
+    const int band0 = band_begin + band_tile * BN;
+    const int iw0 = iw_chunk * NWC;
+    const int nc = p.nc;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int bandw = band0 + warp * RNW;
+    const int nchunks = (nc + KC - 1) / KC;
+    volatile int *abort = &abort_flag;
+
+    // Producer: copy chunk c into stage c % NSTAGE.
+    auto issue = [&](int c) {
+        const int k0 = c * KC;
+        const int cnt = min(KC, nc - k0);
+        const unsigned bytes = (unsigned)cnt * 16u;
+        float4 *st = stage_mem + (c % NSTAGE) * STAGE;
+        unsigned long long *bar = &full_bar[c % NSTAGE];
+        mbar_expect_tx(bar, bytes * (2 * RG + BN));
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const size_t r = (size_t)min(row0 + g, p.ng - 1) * nc + k0;
+            bulk_copy_g2s(st + g * KC, s.rowW + r, bytes, bar);
+            bulk_copy_g2s(st + (RG + g) * KC, s.rowQ + r, bytes, bar);
+        }
+#pragma unroll
+        for (int n = 0; n < BN; ++n) {
+            const size_t b = (size_t)min(band0 + n, band_end - 1) * nc + k0;
+            bulk_copy_g2s(st + (2 * RG + n) * KC, s.band + b, bytes, bar);
+        }
+    };
+
+    __syncthreads();  // the previous tile of this block is done with the barriers
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        for (int i = 0; i < NSTAGE; ++i) {
+            if (reinit) {
+                mbar_inval(&full_bar[i]);
+                mbar_inval(&empty_bar[i]);
+            }
+            mbar_init(&full_bar[i], 1);
+            mbar_init(&empty_bar[i], NWARP);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = 0;  // chunks issued so far (thread 0 only)
+    if (threadIdx.x == 0)
+        for (; issued < NSTAGE - 1 && issued < nchunks; ++issued) issue(issued);
+
+    df wx[RNW][NWC];
+    float pole_thr[RNW][NWC];
+#pragma unroll
+    for (int n = 0; n < RNW; ++n) {
+        const int b = min(bandw + n, band_end - 1);
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
+            wx[n][w] = {x.x, x.y};
+            pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
+        }
+    }
+    df acc[RNW][RG][NWC][2];
+#pragma unroll
+    for (int n = 0; n < RNW; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                acc[n][g][w][0] = {0.f, 0.f};
+                acc[n][g][w][1] = {0.f, 0.f};
+            }
+
+    int c_stop = nchunks;  // first chunk thread 0 did not consume
+    for (int c = 0; c < nchunks; ++c) {
+        // Refill the stage that chunk c - 1 used with chunk c + NSTAGE - 1.
+        if (threadIdx.x == 0 && issued < nchunks && !*abort) {
+            if (SYNC == kSyncBlock || issued < NSTAGE) {
+                if (issued >= NSTAGE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(issued++);
+            } else {
+                const int sp = issued % NSTAGE;
+                const unsigned par = (unsigned)((issued / NSTAGE - 1) & 1);
+                if (mbar_wait(&empty_bar[sp], par, abort)) {
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    issue(issued++);
+                }
+            }
+        }
+        if (SYNC == kSyncRing && warp == 0) __syncwarp();  // warp 0 waits for its producer lane
+        const int sidx = c % NSTAGE;
+        const bool ok = mbar_wait(&full_bar[sidx], (unsigned)((c / NSTAGE) & 1), abort);
+        if (ok) {
+            const float4 *st = stage_mem + sidx * STAGE;      // row planes
+            const float4 *sb = st + (2 * RG + warp * RNW) * KC;  // this warp's bands
+            const int k0 = c * KC;
+            const int cnt = min(KC, nc - k0);
+#pragma unroll 1
+            for (int il = lane; il < cnt; il += 32)
+                mixed_column<RNW, RG, NWC, KC>(p, st, sb, il, k0 + il, row0, bandw, band_end,
+                                               iw0, wx, pole_thr, acc);
+        }
+        if (SYNC == kSyncBlock) {
+            __syncthreads();  // every warp is done with stage sidx
+            if (*abort) {
+                c_stop = c;
+                break;
+            }
+        } else {
+            if (!ok) {
+                c_stop = c;
+                break;
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty_bar[sidx]);
+        }
+    }
+
+    if (__syncthreads_or(*abort)) {
+        if (threadIdx.x == 0) {
+            atomicOr(part.err, kErrPipelineTimeout);
+            // Let the copies still in flight land before the block retires.
+            for (int j = c_stop; j < issued; ++j) {
+                int spin = 0;
+                while (!mbar_try_wait(&full_bar[j % NSTAGE], (unsigned)((j / NSTAGE) & 1)) &&
+                       ++spin < kWaitLimit) {
+                }
+            }
+        }
+        return false;
+    }
+
+    // Warp tree in df arithmetic (fixed order), then one FP64 value per
+    // (band, row, frequency) and component into shared memory.
+#pragma unroll
+    for (int n = 0; n < RNW; ++n)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w)
+#pragma unroll
+                for (int ri = 0; ri < 2; ++ri) {
+                    df v = acc[n][g][w][ri];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const df o = {__shfl_down_sync(0xffffffffu, v.h, off),
+                                      __shfl_down_sync(0xffffffffu, v.l, off)};
+                        v = df_add(v, o);
+                    }
+                    if (lane == 0)
+                        S[(((warp * RNW + n) * RG + g) * NWC + w) * 2 + ri] = to_double(v);
+                }
+    __syncthreads();
+    noflag_epilogue<BN, RG, NWC>(p, part, S, row0, band0, band_end, iw0, tile, row_tile);
+    return true;
+}
+
+}  // namespace gpp

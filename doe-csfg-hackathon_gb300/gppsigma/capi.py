@@ -52,6 +52,9 @@ _SIGS = {
     "gpp_context_destroy": (_i, [_vp]),
     "gpp_sigma_host": (_i, [_vp, C.POINTER(GppProblem), C.POINTER(GppOutputs)]),
     "gpp_sigma_batched": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _i, _vp]),
+    "gpp_batch_create": (_i, [C.POINTER(_vp), C.POINTER(GppProblem), C.POINTER(GppOutputs), _i]),
+    "gpp_batch_run": (_i, [_vp, _vp]),
+    "gpp_batch_destroy": (_i, [_vp]),
     "gpp_sigma_static_scratch": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _vp]),
     "gpp_autotune": (_i, [C.POINTER(GppProblem), _i, _vp, C.POINTER(_i)]),
     "gpp_set_variant": (_i, [_i, _i]),

@@ -189,8 +189,23 @@ gpp_status gpp_sigma_static_scratch(const gpp_problem *problem, const gpp_output
  * Batched states: many independent quasiparticle states (uneven sizes) in
  * one persistent launch over a work queue of (state, band tile, row tile).
  * ------------------------------------------------------------------------ */
+/* One-shot: plans, runs and frees a batch on `stream`; returns when the
+ * results are written.  All problems must share precision, nw and
+ * semantics; outputs are overwritten as in gpp_sigma. */
 gpp_status gpp_sigma_batched(const gpp_problem *problems, const gpp_outputs *outs, int nstates,
                              gpp_stream_t stream);
+
+/* Reusable plan: the work list, device tables and scratch are built once
+ * (gpp_batch_create allocates; the arrays behind the problems' pointers may
+ * change contents between runs but not move).  gpp_batch_run enqueues a run
+ * on `stream`; on a stream other than the legacy/per-thread default the
+ * first run is captured into a CUDA graph and later runs replay it.
+ * gpp_batch_destroy waits for outstanding runs and frees the plan. */
+typedef struct gpp_batch gpp_batch;
+gpp_status gpp_batch_create(gpp_batch **batch, const gpp_problem *problems,
+                            const gpp_outputs *outs, int nstates);
+gpp_status gpp_batch_run(gpp_batch *batch, gpp_stream_t stream);
+gpp_status gpp_batch_destroy(gpp_batch *batch);
 
 /* ------------------------------------------------------------------------
  * Autotuner for the mixed-precision unoccupied-band kernel.  It is compiled
