@@ -191,8 +191,7 @@ def main() -> int:
         dist = dist_mod
     lib = capi.load()
 
-    inp = W.make_inputs(shape, gdist.state_seed(SEED, rank))
-    d = ops.DeviceInputs.from_host(inp)
+    d = ops.device_inputs(shape, gdist.state_seed(SEED, rank))
     stream = torch.cuda.current_stream()
     nterms = shape.terms
     unocc_terms = (shape.number_bands - shape.nvband) * shape.ngpown * shape.ncouls * shape.nw
@@ -275,8 +274,10 @@ def main() -> int:
     arrays = {}
     for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul", "inv_igp_index",
               "indinv", "wx_array"):
-        src = np.ascontiguousarray(getattr(inp, k))
-        arrays[k] = torch.from_numpy(src).pin_memory().numpy()
+        src = getattr(d, k)
+        host = torch.empty(src.shape, dtype=src.dtype, pin_memory=True)
+        host.copy_(src)
+        arrays[k] = host.numpy()
     h2d = int(sum(a.nbytes for a in arrays.values()))
     d2h = 2 * shape.nw * 16
     e2e_times = []

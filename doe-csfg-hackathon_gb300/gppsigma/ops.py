@@ -154,6 +154,17 @@ class DeviceInputs:
                    t(inp.inv_igp_index), t(inp.indinv) if with_indinv else None, t(wx), stride)
 
 
+def device_inputs(shape, seed: int = 20240607, device="cuda") -> DeviceInputs:
+    """Seeded workload generated directly in device memory (same bits as
+    workload.make_inputs, without the host round trip)."""
+    from . import workload
+    t = workload.make_inputs_device(shape, seed, device)
+    stride = 0 if t["wx_array"].shape[0] == 1 and shape.number_bands != 1 else shape.nw
+    return DeviceInputs(shape.number_bands, shape.nvband, shape.ncouls, shape.ngpown, shape.nw,
+                        t["aqsmtemp"], t["aqsntemp"], t["I_eps_array"], t["wtilde_array"],
+                        t["vcoul"], t["inv_igp_index"], t["indinv"], t["wx_array"], stride)
+
+
 @dataclasses.dataclass
 class SigmaResult:
     achtemp: "torch.Tensor"

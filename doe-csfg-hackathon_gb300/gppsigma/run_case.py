@@ -36,15 +36,15 @@ def main() -> int:
     from gppsigma import ops
 
     torch.cuda.set_device(0)
-    inp = W.make_inputs(SHAPES[args.workload], args.seed)
-    d = ops.DeviceInputs.from_host(inp)
+    shape = SHAPES[args.workload]
+    d = ops.device_inputs(shape, args.seed)
     out = None
     for i in range(args.repeat):
         t0 = time.perf_counter()
         out = ops.sigma(d, args.precision, args.semantics, out=out)
         ops.wait()
         dt = time.perf_counter() - t0
-        print(f"step {i}: {dt * 1e3:.2f} ms, {inp.shape.terms / dt:.4e} terms/s")
+        print(f"step {i}: {dt * 1e3:.2f} ms, {shape.terms / dt:.4e} terms/s")
     for iw, z in enumerate(out.achtemp.cpu().numpy()):
         print(f"achtemp[{iw}] = ({z.real:.15g},{z.imag:.15g})")
     for iw, z in enumerate(out.asxtemp.cpu().numpy()):

@@ -209,3 +209,95 @@ def batched_shapes(nstates: int = 64, seed: int = 20240607, scale: float = 1.0) 
         nc = max(20, int(nc * scale))
         out.append(Shape(nb, min(nv, nb), nc, nc // 20, 3))
     return out
+
+
+# ---------------------------------------------------------------------------
+# The same generator on a torch device (bit-identical to the numpy one): the
+# SplitMix64 stream in int64 arithmetic (two's-complement wrap-around, logical
+# shifts via masks), so large workloads are generated where they are used.
+
+def _to_i64(u: int) -> int:
+    u &= 0xFFFFFFFFFFFFFFFF
+    return u - (1 << 64) if u >= (1 << 63) else u
+
+
+def _lsr(z, k: int):
+    import torch
+    return torch.bitwise_and(torch.bitwise_right_shift(z, k), (1 << (64 - k)) - 1)
+
+
+def _mix_t(z):
+    z = torch_bitxor(z, _lsr(z, 30)) * _to_i64(int(_M1))
+    z = torch_bitxor(z, _lsr(z, 27)) * _to_i64(int(_M2))
+    return torch_bitxor(z, _lsr(z, 31))
+
+
+def torch_bitxor(a, b):
+    import torch
+    return torch.bitwise_xor(a, b)
+
+
+def uniform_t(seed: int, stream: int, n: int, lo: float, hi: float, device, out=None):
+    """Device twin of uniform(): the same n doubles, as a float64 tensor."""
+    import torch
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=device)
+    key = _to_i64(int(_key(seed, stream)))
+    golden = _to_i64(int(_GOLDEN))
+    scale = hi - lo
+    chunk = 1 << 26
+    for s in range(0, n, chunk):
+        e = min(n, s + chunk)
+        ctr = torch.arange(s + 1, e + 1, dtype=torch.int64, device=device)
+        z = _mix_t(ctr * golden + key)
+        u = _lsr(z, 11).to(torch.float64) * (1.0 / 9007199254740992.0)
+        out[s:e] = u * scale + lo
+    return out
+
+
+def _complex_t(seed, s_re, s_im, rows, cols, lo_re, hi_re, lo_im, hi_im, device):
+    import torch
+    z = torch.empty((rows, cols), dtype=torch.complex128, device=device)
+    v = torch.view_as_real(z).view(rows * cols, 2)
+    n = rows * cols
+    v[:, 0] = uniform_t(seed, s_re, n, lo_re, hi_re, device)
+    v[:, 1] = uniform_t(seed, s_im, n, lo_im, hi_im, device)
+    return z
+
+
+def make_inputs_device(shape: Shape, seed: int = 20240607, device="cuda") -> dict:
+    """make_inputs() generated directly on `device` (torch tensors, same bits):
+    keys aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul,
+    inv_igp_index, indinv, wx_array."""
+    import torch
+    nb, nc, ng, nw = shape.number_bands, shape.ncouls, shape.ngpown, shape.nw
+    if not (0 <= shape.nvband <= nb and nc > 0 and 0 <= ng <= nc and nw > 0):
+        raise ValueError(f"bad shape {shape}")
+    out = {
+        "aqsmtemp": _complex_t(seed, _S_AQSM_RE, _S_AQSM_IM, nb, nc, -0.5, 0.5, -0.5, 0.5, device),
+        "aqsntemp": _complex_t(seed, _S_AQSN_RE, _S_AQSN_IM, nb, nc, -0.5, 0.5, -0.5, 0.5, device),
+        "I_eps_array": _complex_t(seed, _S_IEPS_RE, _S_IEPS_IM, ng, nc, -0.5, 0.5, -0.5, 0.5, device),
+        "wtilde_array": _complex_t(seed, _S_WT_RE, _S_WT_IM, ng, nc, 0.5, 2.0, -0.05, 0.05, device),
+        "vcoul": uniform_t(seed, _S_VCOUL, nc, 0.1, 1.0, device),
+    }
+    keys = uniform_t(seed, _S_IGP, nc, 0.0, 1.0, device)
+    igp = torch.sort(torch.argsort(keys, stable=True)[:ng]).values.to(torch.int32)
+    if shape.igp_overflow:
+        k = min(shape.igp_overflow, ng)
+        igp[ng - k:] = nc + torch.arange(k, dtype=torch.int32, device=device)
+    out["inv_igp_index"] = igp.contiguous()
+    wx = torch.from_numpy(make_wx(shape, seed)).to(device)
+    if shape.near_pole > 0.0 and ng > 0:
+        n = ng * nc
+        sel = uniform_t(seed, _S_POLE_SEL, n, 0.0, 1.0, device) < shape.near_pole
+        idx = torch.nonzero(sel).flatten()
+        band = torch.clamp((uniform_t(seed, _S_POLE_BAND, n, 0.0, 1.0, device)[idx] * nb).to(torch.int64), max=nb - 1)
+        iwk = torch.clamp((uniform_t(seed, _S_POLE_IW, n, 0.0, 1.0, device)[idx] * nw).to(torch.int64), max=nw - 1)
+        dre = uniform_t(seed, _S_POLE_DRE, n, -7e-5, 7e-5, device)[idx]
+        dim = uniform_t(seed, _S_POLE_DIM, n, -7e-5, 7e-5, device)[idx]
+        flat = torch.view_as_real(out["wtilde_array"]).view(-1, 2)
+        flat[idx, 0] = wx[band, iwk] + dre
+        flat[idx, 1] = dim
+    out["indinv"] = torch.arange(nc, dtype=torch.int32, device=device)
+    out["wx_array"] = wx.contiguous()
+    return out

@@ -57,3 +57,13 @@ def test_batched_shapes_ranges():
     for s in shapes:
         assert 256 <= s.number_bands <= 2048 and 8192 <= s.ncouls <= 65536
         assert 2 <= s.nvband <= 8 and s.ngpown == s.ncouls // 20 and s.nw == 3
+
+
+def test_device_generator_matches_host_generator():
+    torch = __import__("pytest").importorskip("torch")
+    for sh in (W.Shape(12, 2, 1500, 30, 3, near_pole=0.02), W.Shape(5, 1, 257, 7, 4, igp_overflow=2)):
+        a = W.make_inputs(sh, 23)
+        b = W.make_inputs_device(sh, 23, device="cpu")
+        for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul",
+                  "inv_igp_index", "indinv", "wx_array"):
+            np.testing.assert_array_equal(getattr(a, k), b[k].numpy(), err_msg=k)
