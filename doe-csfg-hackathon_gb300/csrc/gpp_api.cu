@@ -248,9 +248,9 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const int nb0 = do_main ? (b0 > p.nv ? b0 : p.nv) : b1, nb1 = b1;
     const bool has_flag = fb1 > fb0 && p.ng > 0;
     const bool has_noflag = nb1 > nb0 && p.ng > 0;
-    const bool mixed = precision == GPP_PRECISION_MIXED && has_noflag;
+    const bool mixed = precision == GPP_PRECISION_MIXED && (has_noflag || has_flag);
 
-    const TileShape fs = flag_shape(p);
+    const TileShape fs = flag_shape(p);  // same tiling for the FP64 and the mixed occupied tile
     const TileShape ns = mixed ? mixed_noflag_shape(p) : fp64_noflag_shape(p);
     const long long rows_f = has_flag ? ceil_div(p.ng, fs.rg) : 0;
     const long long rows_n = has_noflag ? ceil_div(p.ng, ns.rg) : 0;
@@ -294,8 +294,10 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         // Different row tilings: pad the shorter per-band segments with zeros.
         e = cudaMemsetAsync(part.n1, 0, sizeof(double2) * (size_t)(n1_seg * p.nb), s);
     }
+    if (e == cudaSuccess && mixed)  // float-float planes of every band the call touches
+        e = launch_split(p, w + o_split, has_flag ? fb0 : nb0, has_noflag ? nb1 : fb1, s);
     SideStream *side = nullptr;
-    const bool overlap = mixed && has_flag && overlap_occupied();
+    const bool overlap = mixed && has_flag && has_noflag && overlap_occupied();
     if (overlap) {
         st = side_stream(dev, &side);
         if (st != GPP_OK) {
@@ -306,7 +308,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     }
     if (e == cudaSuccess && has_flag && !overlap) {
         part.ach_tile0 = 0;
-        e = launch_flag_fp64(p, part, s);
+        e = mixed ? launch_flag_mixed(p, part, w + o_split, s) : launch_flag_fp64(p, part, s);
     }
     if (e == cudaSuccess && has_noflag) {
         part.ach_tile0 = (int)tiles_f;
@@ -322,7 +324,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     if (e == cudaSuccess && overlap) {
         e = cudaStreamWaitEvent(side->st, side->fork, 0);
         part.ach_tile0 = 0;
-        if (e == cudaSuccess) e = launch_flag_fp64(p, part, side->st);
+        if (e == cudaSuccess) e = launch_flag_mixed(p, part, w + o_split, side->st);
         if (e == cudaSuccess) e = cudaEventRecord(side->join, side->st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, side->join, 0);
     }

@@ -103,8 +103,8 @@ batched_fp64_kernel(const Problem *probs, const Partials *parts, const BatchItem
     }
 }
 
-// Persistent mixed-precision kernel: FP32 unoccupied tiles through the
-// shared-memory pipeline, FP64 occupied tiles in between.
+// Persistent mixed-precision kernel: unoccupied tiles through the
+// shared-memory pipeline, occupied tiles in float-float between them.
 template <int RG, int NWC, int FRG>
 __global__ void __launch_bounds__(kThreads)
 batched_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
@@ -123,15 +123,16 @@ batched_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPla
         const BatchItem bi = items[it];
         const Problem p = probs[bi.state];
         const Partials part = parts[bi.state];
+        const SplitPlanes sp = splits[bi.state];
         if (bi.kind == 0) {
             if (p.semantics == kSemKerSeq)
-                flag_fp64_tile<FRG, NWC, kThreads, kSemKerSeq>(p, part, bi.row_tile, bi.band_tile,
-                                                               bi.iw_chunk, bi.tile, red, S);
+                flag_mixed_tile<FRG, NWC, kThreads, kSemKerSeq>(p, part, sp, bi.row_tile,
+                                                                bi.band_tile, bi.iw_chunk, bi.tile,
+                                                                red, S);
             else
-                flag_fp64_tile<FRG, NWC, kThreads, kSemComplexSeq>(
-                    p, part, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, red, S);
+                flag_mixed_tile<FRG, NWC, kThreads, kSemComplexSeq>(
+                    p, part, sp, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, red, S);
         } else {
-            const SplitPlanes sp = splits[bi.state];
             if (!mixed_tile<1, RG, NWC, 4, 128, 3, kSyncBlock>(p, part, sp, p.nv, p.nb, bi.row_tile,
                                                                bi.band_tile, bi.iw_chunk, bi.tile,
                                                                reinit))
@@ -315,7 +316,7 @@ gpp_status plan_batch(gpp_batch *b, const gpp_problem *problems, const gpp_outpu
             for (int c = 0; c < nchunk; ++c) {
                 for (int band = 0; band < (s.tiles_f ? p.nv : 0); ++band)
                     for (int r = 0; r < s.rows_f; ++r)
-                        flag.push_back({tile_cost * (mixed ? 8.0 : 1.25),
+                        flag.push_back({tile_cost * (mixed ? 1.5 : 1.25),
                                         BatchItem{i, 0, r, band, c, (int)(band * s.rows_f + r)}});
                 const long long bt = s.tiles_n ? s.tiles_n / s.rows_n : 0;
                 for (long long t = 0; t < bt; ++t)
@@ -504,8 +505,8 @@ gpp_status enqueue(gpp_batch *b, cudaStream_t s) {
         if (b->precision == GPP_PRECISION_MIXED)
             for (int i = w.s0; i < w.s1 && e == cudaSuccess; ++i) {
                 const Problem &p = b->probs[i];
-                if (p.nb > p.nv && p.ng > 0) {
-                    e = launch_split(p, b->d_split + w.split_off[i - w.s0], p.nv, p.nb, s);
+                if (p.nb > 0 && p.ng > 0) {
+                    e = launch_split(p, b->d_split + w.split_off[i - w.s0], 0, p.nb, s);
                     launches += 2;
                 }
             }

@@ -47,8 +47,13 @@ cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 // Mixed precision path (gpp_mixed.cu).
 size_t mixed_split_bytes(const Problem &p);
 TileShape mixed_noflag_shape(const Problem &p);
+// The split planes must have been written (launch_split) for the bands used:
+// [band_begin, band_end) for the unoccupied kernel, [0, nvband) for the
+// occupied one.
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws,
                                 int band_begin, int band_end, cudaStream_t s, int variant);
+cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
+                              cudaStream_t s);
 // Pipeline variants of the mixed kernel, selectable per call (autotuner).
 int mixed_variant_count();
 const char *mixed_variant_name(int variant);

@@ -173,12 +173,46 @@ cudaError_t launch_split(const Problem &p, void *split_ws, int b0, int b1, cudaS
     return cudaGetLastError();
 }
 
+template <int RG, int NWC, int THREADS, int SEM>
+__global__ void __launch_bounds__(THREADS)
+flag_mixed_kernel(Problem p, Partials part, SplitPlanes s) {
+    constexpr int K = RG * NWC * 4;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+    flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, blockIdx.x, blockIdx.y, blockIdx.z,
+                                           (long long)blockIdx.y * gridDim.x + blockIdx.x, red, S);
+}
+
+template <int NWC>
+cudaError_t launch_flag_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s,
+                                cudaStream_t st) {
+    dim3 grid(ceil_div(p.ng, 2), p.nv, ceil_div(p.nw, NWC));
+    if (p.semantics == kSemKerSeq)
+        flag_mixed_kernel<2, NWC, 128, kSemKerSeq><<<grid, 128, 0, st>>>(p, part, s);
+    else
+        flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(p, part, s);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
+                              cudaStream_t st) {
+    if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
+    const SplitPlanes s = planes(p, split_ws);
+    switch (nwc_for(p.nw)) {
+        case 1: return launch_flag_mixed_t<1>(p, part, s, st);
+        case 2: return launch_flag_mixed_t<2>(p, part, s, st);
+        case 3: return launch_flag_mixed_t<3>(p, part, s, st);
+        case 4: return launch_flag_mixed_t<4>(p, part, s, st);
+        default: return launch_flag_mixed_t<8>(p, part, s, st);
+    }
+}
+
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws, int b0,
                                 int b1, cudaStream_t st, int variant) {
     if (b1 <= b0 || p.ng == 0) return cudaSuccess;
     const SplitPlanes s = planes(p, split_ws);
-    cudaError_t e = launch_split(p, split_ws, b0, b1, st);
-    if (e != cudaSuccess) return e;
+    cudaError_t e = cudaSuccess;
     switch (nwc_for(p.nw)) {
         case 1: return launch_mixed_t<1, 2, 1, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
         case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);

@@ -119,6 +119,46 @@ __device__ __forceinline__ void noflag_fp64_tile(const Problem &p, const Partial
     noflag_epilogue<RN, RG, NWC>(p, part, S, row0, band0, band_end, iw0, tile, row_tile);
 }
 
+// Epilogue of an occupied-band tile: S holds, per (row g, frequency w), the
+// ig sums of aqsn*sch and aqsn*ssx as S[(g*NWC + w)*4 + {0,1 | 2,3}].  Weight
+// by conj(aqsm[band,igp]) (the matngmatmgp factor) and by 0.5 vcoul[igp]
+// (achtemp) or occ vcoul[igp] (asxtemp), gppComplex_seq.cpp:359-363,378-381;
+// threads 0..NWC-1 write achtemp partials, NWC..2NWC-1 asxtemp partials and
+// thread 64 the iw = 2 column of acht_n1_loc.
+template <int RG, int NWC>
+__device__ __forceinline__ void flag_epilogue(const Problem &p, const Partials &part,
+                                              const double *S, int row0, int band, int iw0,
+                                              long long tile, int row_tile) {
+    const int nc = p.nc;
+    const int t = threadIdx.x;
+    // t < NWC: achtemp partial; NWC <= t < 2 NWC: asxtemp partial; t == 64: n1 column.
+    const bool do_ach = t < NWC, do_asx = t >= NWC && t < 2 * NWC, do_n1 = part.n1 && t == 64;
+    if (do_ach || do_asx || do_n1) {
+        const int w = do_ach ? t : (do_asx ? t - NWC : 2 - iw0);
+        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
+            double2 tot = make_double2(0.0, 0.0);
+#pragma unroll
+            for (int g = 0; g < RG; ++g) {
+                const int row = row0 + g;
+                if (row >= p.ng) continue;
+                const int igp = resolve_igp(p, row, part.err);
+                if (igp < 0) continue;
+                const double2 m = __ldg(p.aqsm + (size_t)band * nc + igp);
+                const int k = (g * NWC + w) * 4 + (do_asx ? 2 : 0);
+                const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
+                const double v_igp = __ldg(p.vcoul + igp);
+                tot = cadd(tot, do_asx ? cscale(s, p.occ * v_igp) : cscale(cscale(s, 0.5), v_igp));
+            }
+            if (do_ach)
+                part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + tile] = tot;
+            else if (do_asx)
+                part.asx[(long long)(iw0 + w) * part.asx_seg + tile] = tot;
+            else
+                part.n1[(long long)band * part.n1_seg + row_tile] = tot;
+        }
+    }
+}
+
 // One occupied-band term of ssxt_scht_solver (gppComplex_seq.cpp:16-63),
 // accumulated as aqsn*sch and aqsn*ssx (the conj(aqsm) factor of
 // matngmatmgp is applied in the epilogue).  cwr = 1/wx^2 for branch A.
@@ -212,34 +252,7 @@ __device__ __forceinline__ void flag_fp64_tile(const Problem &p, const Partials 
             v[k + 3] = acc_x[g][w].y;
         }
     block_reduce<K, THREADS>(v, red, S);
-
-    const int t = threadIdx.x;
-    // t < NWC: achtemp partial; NWC <= t < 2 NWC: asxtemp partial; t == 64: n1 column.
-    const bool do_ach = t < NWC, do_asx = t >= NWC && t < 2 * NWC, do_n1 = part.n1 && t == 64;
-    if (do_ach || do_asx || do_n1) {
-        const int w = do_ach ? t : (do_asx ? t - NWC : 2 - iw0);
-        if (w >= 0 && w < NWC && iw0 + w < p.nw) {
-            double2 tot = make_double2(0.0, 0.0);
-#pragma unroll
-            for (int g = 0; g < RG; ++g) {
-                const int row = row0 + g;
-                if (row >= p.ng) continue;
-                const int igp = resolve_igp(p, row, part.err);
-                if (igp < 0) continue;
-                const double2 m = __ldg(p.aqsm + (size_t)band * nc + igp);
-                const int k = (g * NWC + w) * 4 + (do_asx ? 2 : 0);
-                const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
-                const double v_igp = __ldg(p.vcoul + igp);
-                tot = cadd(tot, do_asx ? cscale(s, p.occ * v_igp) : cscale(cscale(s, 0.5), v_igp));
-            }
-            if (do_ach)
-                part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + tile] = tot;
-            else if (do_asx)
-                part.asx[(long long)(iw0 + w) * part.asx_seg + tile] = tot;
-            else
-                part.n1[(long long)band * part.n1_seg + row_tile] = tot;
-        }
-    }
+    flag_epilogue<RG, NWC>(p, part, S, row0, band, iw0, tile, row_tile);
 }
 
 }  // namespace gpp

@@ -5,6 +5,7 @@
 
 #include "gpp_df.cuh"
 #include "gpp_internal.cuh"
+#include "gpp_tiles_fp64.cuh"
 
 namespace gpp {
 
@@ -329,6 +330,181 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
     __syncthreads();
     noflag_epilogue<BN, RG, NWC>(p, part, S, row0, band0, band_end, iw0, tile, row_tile);
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// Occupied bands (ssxt_scht_solver, gppComplex_seq.cpp:16-63) in float-float.
+
+// a > t for a df value with |a.l| <= ~2^-22 |a.h| and a normalised df
+// threshold t: decided on the high parts unless they are within 1e-5 of each
+// other, then on the exact df difference.  Avoids branch flips at rounding
+// level against the FP64 reference.
+__device__ __forceinline__ bool df_gt(df a, df t) {
+    const float d = fsub(a.h, t.h);
+    if (fabsf(d) > 1e-5f * fabsf(t.h)) return d > 0.f;
+    const df e = df_norm(df_sub(a, t));
+    return e.h > 0.f || (e.h == 0.f && e.l > 0.f);
+}
+__device__ __forceinline__ df df_of(double x) { return split(x); }
+__device__ __forceinline__ df df_abs2(df re, df im) { return df_add(df_sqr(re), df_sqr(im)); }
+// (a.re + i a.im) * (b.re + i b.im) in df.
+__device__ __forceinline__ void df_cmul(df ar, df ai, df br, df bi, df &cr, df &ci) {
+    cr = df_sub(df_mul(ar, br), df_mul(ai, bi));
+    ci = df_add(df_mul(ar, bi), df_mul(ai, br));
+}
+__device__ __forceinline__ df df_scale(df a, float k) { return {fmul(a.h, k), fmul(a.l, k)}; }
+
+// One occupied-band tile in mixed precision: rows row_tile*RG.., one band,
+// frequencies iw_chunk*NWC..; reads the float-float split planes (bands
+// [0, nvband) must have been split too).  Per term, on df values:
+//   wdiff, |wdiff|^2, rden = 1/|wdiff|^2, delwr = |delw|^2 = |wtilde|^2 rden;
+//   branch A (|wdiff|^2 > limittwo, delwr < limitone):
+//     aqsn*sch = A conj(wdiff) rden with A = aqsn Q,  aqsn*ssx = (aqsn Omega2) / wx^2
+//     (the 1/wx^2 factor is applied to the ig sum, in FP64);
+//   branch B (delwr > to1): sch = 0, ssx = -Omega2 conj(cden) delw / |cden|^2,
+//     cden = 4 wtilde^2 (0.5 + delw);
+//   cutoff |ssx|^2 |wtilde|^2 > 16 |Q|^2 (= |ssx| > 4 |I_eps|) when wx < 0
+//   under COMPLEX_SEQ semantics.
+// Terms within 1e-3 |wx| of the pole are computed in FP64 from the inputs.
+template <int RG, int NWC, int THREADS, int SEM>
+__device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials &part,
+                                                const SplitPlanes &s, int row_tile, int band,
+                                                int iw_chunk, long long tile, double *red,
+                                                double *S) {
+    constexpr int K = RG * NWC * 4;
+    const int row0 = row_tile * RG;
+    const int iw0 = iw_chunk * NWC;
+    const int nc = p.nc;
+    const df kLim2 = df_of(kLimitTwo), kLim1 = df_of(kLimitOne), kT1 = df_of(kTo1);
+
+    const float4 *rw[RG];
+    const float4 *rq[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const int r = min(row0 + g, p.ng - 1);
+        rw[g] = s.rowW + (size_t)r * nc;
+        rq[g] = s.rowQ + (size_t)r * nc;
+    }
+    const float4 *bp = s.band + (size_t)band * nc;
+    df wx[NWC], cwr2[NWC];
+    double wx64[NWC], cwr[NWC];
+    float thr[NWC];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w) {
+        wx64[w] = __ldg(p.wx + (size_t)band * p.wx_stride + min(iw0 + w, p.nw - 1));
+        wx[w] = split(wx64[w]);
+        const double c = wx64[w] * wx64[w];
+        cwr[w] = c / (c * c);  // wx^2 / pow(wx^2, 2) (gppComplex_seq.cpp:38-41)
+        cwr2[w] = split(cwr[w] * cwr[w]);
+        thr[w] = 1e-6f * wx[w].h * wx[w].h;
+    }
+    // Accumulators: aqsn*sch, sum of aqsn*Omega2 over branch-A terms (times
+    // 1/wx^2 later), aqsn*ssx of branch-B and pole terms.
+    df as_r[RG][NWC], as_i[RG][NWC], xa_r[RG][NWC], xa_i[RG][NWC], xb_r[RG][NWC], xb_i[RG][NWC];
+#pragma unroll
+    for (int g = 0; g < RG; ++g)
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            as_r[g][w] = as_i[g][w] = xa_r[g][w] = xa_i[g][w] = xb_r[g][w] = xb_i[g][w] =
+                df{0.f, 0.f};
+        }
+
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        const float4 av = __ldg(bp + ig);
+        const df ar = {av.x, av.y}, ai = {av.z, av.w};
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const float4 wv = __ldg(rw[g] + ig);
+            const float4 qv = __ldg(rq[g] + ig);
+            const df wtr = {wv.x, wv.y}, wti = {wv.z, wv.w}, qr = {qv.x, qv.y}, qi = {qv.z, qv.w};
+            const df wti2 = df_sqr(wti);
+            const df awt2 = df_add(df_sqr(wtr), wti2);                         // |wtilde|^2
+            df w2r, w2i;                                                          // wtilde^2
+            df_cmul(wtr, wti, wtr, wti, w2r, w2i);
+            df omr, omi;                                                          // Omega2 = wtilde Q
+            df_cmul(wtr, wti, qr, qi, omr, omi);
+            const df cut_rhs = df_scale(df_abs2(qr, qi), 16.f);                  // 16 |Q|^2
+            const df om_wt = df_mul(df_abs2(omr, omi), awt2);                   // |Omega2|^2 |wtilde|^2
+            df Ar, Ai, Br, Bi;
+            df_cmul(ar, ai, qr, qi, Ar, Ai);                                      // aqsn Q
+            df_cmul(ar, ai, omr, omi, Br, Bi);                                    // aqsn Omega2
+            const df Ai_wti = df_mul(Ai, wti), Ar_wti = df_mul(Ar, wti);
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const df wr = df_norm(df_sub(wx[w], wtr));   // Re(wdiff); Im(wdiff) = -wti
+                const df d = df_add(df_sqr(wr), wti2);       // |wdiff|^2
+                if (d.h < thr[w]) {
+                    // Near the pole: the whole term in FP64 from the inputs.
+                    const int row = min(row0 + g, p.ng - 1);
+                    const double2 wt = __ldg(p.wt + (size_t)row * nc + ig);
+                    const double2 ie = __ldg(p.ieps + (size_t)row * nc + ig);
+                    const double2 a = __ldg(p.aqsn + (size_t)band * nc + ig);
+                    const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
+                    double2 s64 = make_double2(0.0, 0.0), x64 = make_double2(0.0, 0.0);
+                    flag_term<SEM>(wx64[w], cwr[w], wt, wt2, cmul(wt2, ie), ie, a, s64, x64);
+                    as_r[g][w] = df_add(as_r[g][w], split(s64.x));
+                    as_i[g][w] = df_add(as_i[g][w], split(s64.y));
+                    xb_r[g][w] = df_add(xb_r[g][w], split(x64.x));
+                    xb_i[g][w] = df_add(xb_i[g][w], split(x64.y));
+                    continue;
+                }
+                const df rden = df_rcp(d);
+                const df delwr = df_mul(awt2, rden);
+                if (df_gt(d, kLim2) && df_gt(kLim1, delwr)) {
+                    // Branch A: aqsn*sch = A conj(wdiff) rden; aqsn*ssx = B / wx^2.
+                    const df tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), rden);
+                    const df tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), rden);
+                    as_r[g][w] = df_add(as_r[g][w], tre);
+                    as_i[g][w] = df_add(as_i[g][w], tim);
+                    const bool cut = SEM == kSemComplexSeq && wx64[w] < 0.0 &&
+                                     df_gt(df_mul(om_wt, cwr2[w]), cut_rhs);
+                    if (!cut) {
+                        xa_r[g][w] = df_add(xa_r[g][w], Br);
+                        xa_i[g][w] = df_add(xa_i[g][w], Bi);
+                    }
+                } else if (df_gt(delwr, kT1)) {
+                    // Branch B.  delw = wtilde conj(wdiff) rden, conj(wdiff) = (wr, wti).
+                    df dr, di;
+                    df_cmul(wtr, wti, wr, wti, dr, di);
+                    dr = df_mul(dr, rden);
+                    di = df_mul(di, rden);
+                    df cr, ci;                                   // cden = 4 wtilde^2 (0.5 + delw)
+                    df_cmul(w2r, w2i, df_add(dr, df{0.5f, 0.f}), di, cr, ci);
+                    cr = df_scale(cr, 4.f);
+                    ci = df_scale(ci, 4.f);
+                    const df r2 = df_rcp(df_norm(df_abs2(cr, ci)));
+                    df tr, ti;                                   // -Omega2 conj(cden)
+                    df_cmul(omr, omi, cr, df{-ci.h, -ci.l}, tr, ti);
+                    df sr, si;                                   // ssx = -(...) (delw r2)
+                    df_cmul(tr, ti, df_mul(dr, r2), df_mul(di, r2), sr, si);
+                    sr = df{-sr.h, -sr.l};
+                    si = df{-si.h, -si.l};
+                    const bool cut = SEM == kSemComplexSeq && wx64[w] < 0.0 &&
+                                     df_gt(df_mul(df_abs2(sr, si), awt2), cut_rhs);
+                    if (!cut) {
+                        df pr, pi;
+                        df_cmul(ar, ai, sr, si, pr, pi);
+                        xb_r[g][w] = df_add(xb_r[g][w], pr);
+                        xb_i[g][w] = df_add(xb_i[g][w], pi);
+                    }
+                }
+            }
+        }
+    }
+
+    double v[K];
+#pragma unroll
+    for (int g = 0; g < RG; ++g)
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            const int k = (g * NWC + w) * 4;
+            v[k] = to_double(as_r[g][w]);
+            v[k + 1] = to_double(as_i[g][w]);
+            v[k + 2] = to_double(xa_r[g][w]) * cwr[w] + to_double(xb_r[g][w]);
+            v[k + 3] = to_double(xa_i[g][w]) * cwr[w] + to_double(xb_i[g][w]);
+        }
+    block_reduce<K, THREADS>(v, red, S);
+    flag_epilogue<RG, NWC>(p, part, S, row0, band, iw0, tile, row_tile);
 }
 
 }  // namespace gpp
