@@ -103,15 +103,41 @@ batched_fp64_kernel(const Problem *probs, const Partials *parts, const BatchItem
     }
 }
 
-// Persistent mixed-precision kernel: unoccupied tiles through the
-// shared-memory pipeline, occupied tiles in float-float between them.
-template <int RG, int NWC, int FRG>
+// Persistent mixed-precision kernels: occupied-band tiles (float-float,
+// register-heavy) and unoccupied-band tiles (shared-memory pipeline) run as
+// two launches so each keeps its own occupancy.
+template <int NWC, int FRG>
 __global__ void __launch_bounds__(kThreads)
-batched_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
-                     const BatchItem *items, int n_items, int *head) {
+batched_flag_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
+                          const BatchItem *items, int n_items, int *head) {
     constexpr int KF = FRG * NWC * 4;
     __shared__ double red[(kThreads / 32) * KF];
     __shared__ double S[KF];
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(head, 1);
+        __syncthreads();
+        const int it = s_item;
+        __syncthreads();
+        if (it >= n_items) return;
+        const BatchItem bi = items[it];
+        const Problem p = probs[bi.state];
+        const Partials part = parts[bi.state];
+        const SplitPlanes sp = splits[bi.state];
+        if (p.semantics == kSemKerSeq)
+            flag_mixed_tile<FRG, NWC, kThreads, kSemKerSeq>(p, part, sp, bi.row_tile, bi.band_tile,
+                                                            bi.iw_chunk, bi.tile, red, S);
+        else
+            flag_mixed_tile<FRG, NWC, kThreads, kSemComplexSeq>(
+                p, part, sp, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, red, S);
+        __syncthreads();
+    }
+}
+
+template <int RG, int NWC>
+__global__ void __launch_bounds__(kThreads)
+batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
+                            const BatchItem *items, int n_items, int *head) {
     __shared__ int s_item;
     bool reinit = false;
     for (;;) {
@@ -124,21 +150,11 @@ batched_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPla
         const Problem p = probs[bi.state];
         const Partials part = parts[bi.state];
         const SplitPlanes sp = splits[bi.state];
-        if (bi.kind == 0) {
-            if (p.semantics == kSemKerSeq)
-                flag_mixed_tile<FRG, NWC, kThreads, kSemKerSeq>(p, part, sp, bi.row_tile,
-                                                                bi.band_tile, bi.iw_chunk, bi.tile,
-                                                                red, S);
-            else
-                flag_mixed_tile<FRG, NWC, kThreads, kSemComplexSeq>(
-                    p, part, sp, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, red, S);
-        } else {
-            if (!mixed_tile<1, RG, NWC, 4, 128, 3, kSyncBlock>(p, part, sp, p.nv, p.nb, bi.row_tile,
-                                                               bi.band_tile, bi.iw_chunk, bi.tile,
-                                                               reinit))
-                return;  // abandoned after a bounded wait; the fault bit is set
-            reinit = true;
-        }
+        if (!mixed_tile<1, RG, NWC, 4, 128, 2, kSyncBlock>(p, part, sp, p.nv, p.nb, bi.row_tile,
+                                                           bi.band_tile, bi.iw_chunk, bi.tile,
+                                                           reinit))
+            return;  // abandoned after a bounded wait; the fault bit is set
+        reinit = true;
         __syncthreads();
     }
 }
@@ -168,7 +184,7 @@ struct gpp_batch {
     std::vector<BatchItem> items;
     struct Wave {
         int s0, s1;      // states [s0, s1)
-        int i0, i1;      // items [i0, i1)
+        int i0, i_mid, i1;  // occupied items [i0, i_mid), unoccupied [i_mid, i1)
         size_t split_bytes;
         std::vector<size_t> split_off;  // per state in the wave
     };
@@ -192,7 +208,8 @@ struct gpp_batch {
     std::vector<std::pair<double2 *, size_t>> n1_zero;
     int launches_per_run = 0;
     size_t smem = 0;  // persistent kernel: dynamic shared memory per block
-    int grid = 1;     // persistent kernel: resident blocks on the device
+    int grid = 1;       // persistent kernels: resident blocks on the device
+    int grid_flag = 1;
     cudaGraphExec_t graph = nullptr;
     int *err = nullptr;
 };
@@ -300,7 +317,7 @@ gpp_status plan_batch(gpp_batch *b, const gpp_problem *problems, const gpp_outpu
     } else {
         wave_states.push_back({0, nstates});
     }
-    const size_t off_heads = reserve(sizeof(int) * wave_states.size());
+    const size_t off_heads = reserve(sizeof(int) * 2 * wave_states.size());
     // Items per wave.
     for (auto &ws : wave_states) {
         gpp_batch::Wave w;
@@ -333,14 +350,9 @@ gpp_status plan_batch(gpp_batch *b, const gpp_problem *problems, const gpp_outpu
         };
         std::stable_sort(flag.begin(), flag.end(), by_cost);
         std::stable_sort(unocc.begin(), unocc.end(), by_cost);
-        // Spread the occupied-band items evenly through the unoccupied ones.
-        const size_t nf = flag.size(), nu = unocc.size();
-        size_t fi = 0;
-        for (size_t ui = 0; ui <= nu; ++ui) {
-            while (fi < nf && (double)fi * (double)(nu + 1) <= (double)ui * (double)nf) b->items.push_back(flag[fi++].second);
-            if (ui < nu) b->items.push_back(unocc[ui].second);
-        }
-        while (fi < nf) b->items.push_back(flag[fi++].second);
+        for (auto &f : flag) b->items.push_back(f.second);
+        w.i_mid = (int)b->items.size();
+        for (auto &u : unocc) b->items.push_back(u.second);
         w.i1 = (int)b->items.size();
         b->waves.push_back(w);
     }
@@ -442,23 +454,24 @@ gpp_status upload_tables(gpp_batch *b, int *fault_word) {
     return GPP_OK;
 }
 
-// Launch configuration of the persistent kernel for a frequency chunk NWC:
+// Launch configuration of the persistent kernels for a frequency chunk NWC:
 // dynamic shared memory (opted in here, outside any stream capture) and the
-// resident grid size.
+// resident grid sizes.
 template <int NWC>
-cudaError_t prepare_persistent(int precision, size_t *smem, int *grid) {
-    if (precision == GPP_PRECISION_MIXED) {
+cudaError_t prepare_persistent(gpp_batch *b) {
+    if (b->precision == GPP_PRECISION_MIXED) {
         constexpr int RG = NWC <= 4 ? 2 : 1;
-        auto kern = batched_mixed_kernel<RG, NWC, 2>;
-        *smem = sizeof(float4) * 3 * (2 * RG + 4) * 128;
+        auto kern = batched_noflag_mixed_kernel<RG, NWC>;
+        b->smem = sizeof(float4) * 2 * (2 * RG + 4) * 128;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)*smem);
+                                             (int)b->smem);
         if (e != cudaSuccess) return e;
-        *grid = resident_blocks(kern, *smem);
+        b->grid = resident_blocks(kern, b->smem);
+        b->grid_flag = resident_blocks(batched_flag_mixed_kernel<NWC, 2>, 0);
     } else {
         constexpr int RN = NWC <= 4 ? 4 : 2;
-        *smem = 0;
-        *grid = resident_blocks(batched_fp64_kernel<RN, 2, NWC>, 0);
+        b->smem = 0;
+        b->grid = b->grid_flag = resident_blocks(batched_fp64_kernel<RN, 2, NWC>, 0);
     }
     return cudaGetLastError();
 }
@@ -466,36 +479,46 @@ cudaError_t prepare_persistent(int precision, size_t *smem, int *grid) {
 template <int NWC>
 cudaError_t launch_persistent(gpp_batch *b, int wave, cudaStream_t s) {
     const auto &w = b->waves[wave];
-    const int n = w.i1 - w.i0;
-    if (n <= 0) return cudaSuccess;
-    const BatchItem *items = b->d_items + w.i0;
-    int *head = b->d_heads + wave;
-    const int grid = std::min(n, b->grid);
+    int *heads = b->d_heads + 2 * wave;
+    cudaError_t e = cudaSuccess;
     if (b->precision == GPP_PRECISION_MIXED) {
         constexpr int RG = NWC <= 4 ? 2 : 1;
-        batched_mixed_kernel<RG, NWC, 2><<<grid, kThreads, b->smem, s>>>(
-            b->d_probs, b->d_parts, b->d_splits, items, n, head);
+        const int nf = w.i_mid - w.i0, nu = w.i1 - w.i_mid;
+        if (nf > 0) {
+            batched_flag_mixed_kernel<NWC, 2><<<std::min(nf, b->grid_flag), kThreads, 0, s>>>(
+                b->d_probs, b->d_parts, b->d_splits, b->d_items + w.i0, nf, heads);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && nu > 0) {
+            batched_noflag_mixed_kernel<RG, NWC><<<std::min(nu, b->grid), kThreads, b->smem, s>>>(
+                b->d_probs, b->d_parts, b->d_splits, b->d_items + w.i_mid, nu, heads + 1);
+            e = cudaGetLastError();
+        }
     } else {
         constexpr int RN = NWC <= 4 ? 4 : 2;
-        batched_fp64_kernel<RN, 2, NWC><<<grid, kThreads, 0, s>>>(b->d_probs, b->d_parts, items,
-                                                                   n, head);
+        const int n = w.i1 - w.i0;
+        if (n > 0) {
+            batched_fp64_kernel<RN, 2, NWC><<<std::min(n, b->grid), kThreads, 0, s>>>(
+                b->d_probs, b->d_parts, b->d_items + w.i0, n, heads);
+            e = cudaGetLastError();
+        }
     }
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t prepare(gpp_batch *b) {
     switch (b->nw <= 4 ? b->nw : 8) {
-        case 1: return prepare_persistent<1>(b->precision, &b->smem, &b->grid);
-        case 2: return prepare_persistent<2>(b->precision, &b->smem, &b->grid);
-        case 3: return prepare_persistent<3>(b->precision, &b->smem, &b->grid);
-        case 4: return prepare_persistent<4>(b->precision, &b->smem, &b->grid);
-        default: return prepare_persistent<8>(b->precision, &b->smem, &b->grid);
+        case 1: return prepare_persistent<1>(b);
+        case 2: return prepare_persistent<2>(b);
+        case 3: return prepare_persistent<3>(b);
+        case 4: return prepare_persistent<4>(b);
+        default: return prepare_persistent<8>(b);
     }
 }
 
 // Enqueue one full run of the batch on stream s.
 gpp_status enqueue(gpp_batch *b, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(b->d_heads, 0, sizeof(int) * b->waves.size(), s);
+    cudaError_t e = cudaMemsetAsync(b->d_heads, 0, sizeof(int) * 2 * b->waves.size(), s);
     for (size_t k = 0; k < b->n1_zero.size() && e == cudaSuccess; ++k)
         e = cudaMemsetAsync(b->n1_zero[k].first, 0, b->n1_zero[k].second, s);
     int launches = 0;
@@ -518,7 +541,7 @@ gpp_status enqueue(gpp_batch *b, cudaStream_t s) {
             case 4: e = launch_persistent<4>(b, (int)wv, s); break;
             default: e = launch_persistent<8>(b, (int)wv, s); break;
         }
-        ++launches;
+        launches += 2;
     }
     for (size_t k = 0; k < b->achs.size() && e == cudaSuccess; ++k) {
         e = launch_achstemp(b->probs[b->achs[k].first], b->achs[k].second, b->err, s);

@@ -152,7 +152,7 @@ int mixed_variant_count() { return kNumMixedVariants; }
 const char *mixed_variant_name(int v) {
     return (v >= 0 && v < kNumMixedVariants) ? kMixedVariants[v].name : "default";
 }
-int mixed_default_variant() { return 1; }
+int mixed_default_variant() { return 0; }
 
 size_t mixed_split_bytes(const Problem &p) {
     return sizeof(float4) * ((size_t)2 * p.ng * p.nc + (size_t)p.nb * p.nc) +
