@@ -100,13 +100,29 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def profile_traffic(kernel: str, workload: str):
-    """dram bytes per launch recorded in profiles/ by an ncu capture."""
-    path = os.path.join(REPO, "profiles", f"ncu_{kernel}_{workload}.txt")
+def profile_traffic(kernel: str, workload: str, precision: str):
+    """DRAM bytes (read + write) per launch of `kernel` at `workload`, from the
+    ncu launch-list summary committed in profiles/ (None when not captured)."""
+    path = os.path.join(REPO, "profiles", f"launches_{workload}_{precision}.txt")
     if not os.path.exists(path):
         return None
-    m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
-    return float(m.group(1)) if m else None
+    for line in open(path):
+        m = re.match(rf"\s*{kernel}\S*\s.*dram_bytes_per_launch=([0-9.eE+]+)", line)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def profile_pipe(kernel_file: str, metric: str):
+    """A pipe-utilisation percentage from a committed ncu summary."""
+    path = os.path.join(REPO, "profiles", kernel_file)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith(metric):
+            m = re.search(r"([0-9.]+)\s*%", line)
+            return float(m.group(1)) if m else None
+    return None
 
 
 def run_reference(args, shape: W.Shape) -> dict:
@@ -365,14 +381,14 @@ def main() -> int:
     d2h = 2 * shape.nw * 16
     e2e_times = []
     with ops.HostContext() as ctx:
-        for i in range(2 + max(2, args.steps // 3)):
+        for i in range(2 + max(5, args.steps // 2)):
             barrier()
             t0 = time.perf_counter()
             ctx.sigma(arrays, shape, precision)
             dt = time.perf_counter() - t0
             if i >= 2:
                 e2e_times.append(dt)
-    e2e_s = gdist.max_over_ranks(statistics.mean(e2e_times), dist, "cuda")
+    e2e_s = gdist.max_over_ranks(statistics.median(e2e_times), dist, "cuda")
 
     if rank != 0:
         dist.destroy_process_group()
@@ -383,8 +399,11 @@ def main() -> int:
     flops = unocc_terms * (FLOPS_PER_TERM_BASE + FLOPS_PER_TRIPLE / shape.nw)
     peak = fp32_peak if precision == "mixed" else fp64_peak
     achieved = flops / (kms * 1e-3) * 1e-12 if kms else None
-    kname = "noflag_mixed" if precision == "mixed" else "noflag_fp64"
-    traffic = profile_traffic(kname, args.workload)
+    kname = "mixed_noflag_kernel" if precision == "mixed" else "noflag_fp64_kernel"
+    traffic = profile_traffic(kname, args.workload, precision)
+    pipe_file = "ncu_noflag_mixed_profile.txt" if precision == "mixed" else "ncu_noflag_fp64_profile.txt"
+    pipe_metric = "sm__inst_executed_pipe_fma" if precision == "mixed" else "sm__inst_executed_pipe_fp64"
+    pipe_pct = profile_pipe(pipe_file, pipe_metric)
     roofline = {"bound": "fp32" if precision == "mixed" else "fp64",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if (achieved and peak) else None,
@@ -393,6 +412,10 @@ def main() -> int:
                                "(gpp_probe_fma_peaks), " + ("FP32" if precision == "mixed" else "FP64"),
                 "flops_per_term": FLOPS_PER_TERM_BASE + FLOPS_PER_TRIPLE / shape.nw,
                 "kernel": kname, "kernel_ms": kms,
+                "ncu_pipe_busy_pct": pipe_pct,
+                "ncu_pipe_note": f"{pipe_metric} from profiles/{pipe_file} (profile shape)",
+                "traffic_note": "dram read+write bytes per launch at this workload, "
+                                f"profiles/launches_{args.workload}_{precision}.txt",
                 "fp64_fma_peak_tflops": fp64_peak, "fp32_fma_peak_tflops": fp32_peak}
 
     line = {"metric": METRIC, "value": ws * nterms / (ms * 1e-3), "unit": "terms/s",
@@ -407,7 +430,8 @@ def main() -> int:
             "gpu_launches": int(launches),
             "clocks": clk,
             "e2e": {"value": ws * nterms / e2e_s, "unit": "terms/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                    "path": "gpp_sigma_host from pinned host buffers (median of steps)"},
             "roofline": roofline}
     if fp64_leg:
         line["fp64"] = fp64_leg
