@@ -2,12 +2,13 @@
 //
 // A batch plan lists every tile of every state -- occupied-band tiles (one
 // band x RG rows) and unoccupied-band tiles (RN bands x RG rows), for each
-// frequency chunk -- as work items, ordered longest first and with the FP64
-// occupied-band items spread through the list so they share SMs with the
-// FP32 mixed-precision items.  A persistent grid (SMs x resident blocks)
-// pops items from a global counter; each item writes its partial sums to a
-// fixed slot, so the result does not depend on which block ran which item,
-// and one batched fixed-order reduction produces every state's outputs.
+// frequency chunk -- as work items in two lists, each ordered longest first.
+// Each list runs as its own persistent launch (resident blocks x SMs) whose
+// blocks pop items from a global counter: the occupied-band tile keeps its
+// branchy body and register count out of the unoccupied-band kernel.  Each
+// item writes its partial sums to a fixed slot, so the result does not
+// depend on which block ran which item, and one batched fixed-order
+// reduction produces every state's outputs.
 //
 // Mixed precision needs each state's float-float split planes; states are
 // grouped into waves whose planes fit a workspace budget, and each wave runs
