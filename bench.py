@@ -346,13 +346,7 @@ def main() -> int:
             variant = None
     clocks = ClockSampler(local)
     clocks.start()
-    try:
-        res, ms, kern_ms, launches = timed(precision, args.steps, args.warmup)
-    except capi.GppError as e:
-        if precision != "mixed" or e.status != capi.GPP_ERR_CUDA:
-            raise
-        precision = "fp64"
-        res, ms, kern_ms, launches = timed(precision, args.steps, args.warmup)
+    res, ms, kern_ms, launches = timed(precision, args.steps, args.warmup)
     clk = clocks.stop()
 
     fp64_leg = None

@@ -461,7 +461,7 @@ gpp_status upload_tables(gpp_batch *b, int *fault_word) {
 template <int NWC>
 cudaError_t prepare_persistent(gpp_batch *b) {
     if (b->precision == GPP_PRECISION_MIXED) {
-        constexpr int RG = NWC <= 4 ? 2 : 1;
+        constexpr int RG = 2;  // one row pair of the split planes
         auto kern = batched_noflag_mixed_kernel<RG, NWC>;
         b->smem = sizeof(float4) * 2 * (2 * RG + 4) * 128;
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -483,7 +483,7 @@ cudaError_t launch_persistent(gpp_batch *b, int wave, cudaStream_t s) {
     int *heads = b->d_heads + 2 * wave;
     cudaError_t e = cudaSuccess;
     if (b->precision == GPP_PRECISION_MIXED) {
-        constexpr int RG = NWC <= 4 ? 2 : 1;
+        constexpr int RG = 2;  // one row pair of the split planes
         const int nf = w.i_mid - w.i0, nu = w.i1 - w.i_mid;
         if (nf > 0) {
             batched_flag_mixed_kernel<NWC, 2><<<std::min(nf, b->grid_flag), kThreads, 0, s>>>(

@@ -1,0 +1,132 @@
+// gpp_df2.cuh -- two float-float ("df") lanes per operation, on the packed
+// FP32 instructions of sm_100+ (add/sub/mul/fma .f32x2: one instruction
+// issues two independent FP32 operations).  A df2 value holds two df numbers
+// in structure-of-arrays form, {h.x + l.x, h.y + l.y}, so every step of the
+// df algorithms in gpp_df.cuh becomes one packed instruction for both lanes.
+// Per lane the results are bit-identical to the scalar df functions: the
+// packed operations round each component exactly like __fadd_rn, __fmul_rn
+// and __fmaf_rn, and like those they are never contracted by the compiler.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gpp_df.cuh"
+
+namespace gpp {
+
+struct df2 {
+    float2 h, l;
+};
+
+__host__ __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__host__ __device__ __forceinline__ float2 f2neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__host__ __device__ __forceinline__ float2 f2add(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+// a - b as a + (-b): exact negation folds into the packed add's operand, and
+// (unlike an inline-asm sub.f32x2) lets a lane-broadcast operand be read
+// without first copying it into a register pair.
+__host__ __device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+#ifdef __CUDA_ARCH__
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+__host__ __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+#ifdef __CUDA_ARCH__
+    return __ffma2_rn(a, b, c);
+#else
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+
+// Both lanes hold the same df value.
+__host__ __device__ __forceinline__ df2 df2_bcast(df a) { return {f2(a.h, a.h), f2(a.l, a.l)}; }
+__host__ __device__ __forceinline__ df df2_lane(const df2 &a, int i) {
+    return i == 0 ? df{a.h.x, a.l.x} : df{a.h.y, a.l.y};
+}
+__host__ __device__ __forceinline__ void df2_set_lane(df2 &a, int i, df v) {
+    if (i == 0) {
+        a.h.x = v.h;
+        a.l.x = v.l;
+    } else {
+        a.h.y = v.h;
+        a.l.y = v.l;
+    }
+}
+
+// TwoSum (Knuth) on both lanes.
+__host__ __device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+    const float2 s = f2add(a, b);
+    const float2 bb = f2sub(s, a);
+    const float2 e = f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+    return {s, e};
+}
+__host__ __device__ __forceinline__ df2 df2_add(const df2 &a, const df2 &b) {
+    df2 s = two_sum2(a.h, b.h);
+    s.l = f2add(s.l, f2add(a.l, b.l));
+    return s;
+}
+// TwoSum of a + (-b), written without the negation; per lane bit-identical
+// to two_sum(a, -b).
+__host__ __device__ __forceinline__ df2 two_diff2(float2 a, float2 b) {
+    const float2 s = f2sub(a, b);
+    const float2 bb = f2sub(s, a);
+    const float2 e = f2sub(f2sub(a, f2sub(s, bb)), f2add(b, bb));
+    return {s, e};
+}
+__host__ __device__ __forceinline__ df2 df2_sub(const df2 &a, const df2 &b) {
+    df2 s = two_diff2(a.h, b.h);
+    s.l = f2add(s.l, f2sub(a.l, b.l));
+    return s;
+}
+// (a.h + a.l)(b.h + b.l) without the l*l term (FMA TwoProduct for h*h).
+__host__ __device__ __forceinline__ df2 df2_mul(const df2 &a, const df2 &b) {
+    const float2 p = f2mul(a.h, b.h);
+    float2 e = f2fma(a.h, b.h, f2neg(p));
+    e = f2fma(a.h, b.l, e);
+    e = f2fma(a.l, b.h, e);
+    return {p, e};
+}
+// (h + l)^2 including l*l, so the square stays accurate when l is a sizeable
+// fraction of h (an unnormalised difference after cancellation).
+__host__ __device__ __forceinline__ df2 df2_sqr_full(const df2 &a) {
+    const float2 p = f2mul(a.h, a.h);
+    float2 e = f2fma(a.h, a.h, f2neg(p));
+    e = f2fma(f2add(a.h, a.h), a.l, e);
+    e = f2fma(a.l, a.l, e);
+    return {p, e};
+}
+// 1/d per lane: hardware reciprocal seed (MUFU, relative error ~2^-23) and
+// one Newton-Raphson correction against the full df value.  The seed is
+// taken of fl(d.h + d.l), not of d.h: d may be unnormalised (|d.l| up to
+// ~1e-4 |d.h| after a cancelling wdiff), and one Newton step leaves the
+// square of the seed's relative error.
+__host__ __device__ __forceinline__ df2 df2_rcp(const df2 &d) {
+    const float2 s = f2add(d.h, d.l);
+    float2 r;
+#ifdef __CUDA_ARCH__
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.x) : "f"(s.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.y) : "f"(s.y));
+#else
+    r = make_float2(1.0f / s.x, 1.0f / s.y);
+#endif
+    float2 e = f2fma(f2neg(d.h), r, f2(1.0f, 1.0f));
+    e = f2fma(f2neg(d.l), r, e);
+    return {r, f2mul(r, e)};
+}
+
+}  // namespace gpp

@@ -10,8 +10,9 @@
 // "Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005).  Rounding
 // errors of the main path are captured exactly; only second-order cross
 // terms round in FP32, so each term carries ~2^-44 relative error, far below
-// the 1e-8 target, while costing ~85 FP32 instructions instead of ~11 FP64
-// ones (~700 FP32-equivalents).
+// the 1e-8 target.  A block's two G' rows are the two lanes of the packed
+// f32x2 instructions (gpp_df2.cuh), so a term costs ~44 packed FP32
+// instructions instead of ~11 FP64 ones (~700 FP32-equivalents).
 //
 // FP64 is kept where stability needs it:
 //  * the input conversion: a prep pass computes Q = wtilde * I_eps in FP64 and
@@ -22,10 +23,9 @@
 //    division, the products) is recomputed in FP64 from the original inputs;
 //  * the cross-thread, cross-block and final sums (FP64 trees, fixed order).
 //
-// Work decomposition matches the FP64 kernel (RG rows x RN bands x NWC
-// frequencies per block, threads striding over ig, 16-byte vector loads) with
-// a grouped tile order so that GROUP row tiles stay resident in L2 while all
-// band tiles stream past them.
+// Work decomposition: a block owns one row pair x 4 bands x NWC frequencies,
+// threads stride over ig, and a grouped tile order keeps GROUP row tiles
+// resident in L2 while all band tiles stream past them.
 #include "gpp_kernels.h"
 #include "gpp_tiles_mixed.cuh"
 
@@ -33,26 +33,34 @@ namespace gpp {
 
 namespace {
 
+size_t row_pair_elems(const Problem &p) { return (size_t)((p.ng + 1) / 2) * 4 * p.nc; }
+
 SplitPlanes planes(const Problem &p, void *ws) {
-    char *w = static_cast<char *>(ws);
     SplitPlanes s;
-    const size_t rows = (size_t)p.ng * p.nc, bands = (size_t)p.nb * p.nc;
-    s.rowW = reinterpret_cast<float4 *>(w);
-    s.rowQ = s.rowW + rows;
-    s.band = s.rowQ + rows;
-    s.wx = reinterpret_cast<float2 *>(s.band + bands);
+    s.rows = static_cast<float4 *>(ws);
+    s.band = s.rows + row_pair_elems(p);
+    s.wx = reinterpret_cast<float2 *>(s.band + (size_t)p.nb * p.nc);
     return s;
 }
 
+// One thread per (row pair, ig): Q = wtilde * I_eps in FP64 for both rows,
+// then the hi/lo splits interleaved by row (the row-pair plane layout).
 __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s) {
-    const size_t n = (size_t)p.ng * p.nc;
+    const size_t nc = (size_t)p.nc;
+    const size_t n = (size_t)((p.ng + 1) / 2) * nc;
     for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
-        const double2 wt = __ldg(p.wt + i);
-        const double2 ie = __ldg(p.ieps + i);
-        const double2 q = cmul(wt, ie);
-        const df wr = split(wt.x), wi = split(wt.y), qr = split(q.x), qi = split(q.y);
-        s.rowW[i] = make_float4(wr.h, wr.l, wi.h, wi.l);
-        s.rowQ[i] = make_float4(qr.h, qr.l, qi.h, qi.l);
+        const size_t j = i / nc, ig = i - j * nc;
+        const size_t r0 = 2 * j, r1 = min(2 * j + 1, (size_t)p.ng - 1);
+        const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
+        const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
+        const double2 q1 = cmul(wt1, __ldg(p.ieps + r1 * nc + ig));
+        const df a0 = split(wt0.x), a1 = split(wt1.x), b0 = split(wt0.y), b1 = split(wt1.y);
+        const df c0 = split(q0.x), c1 = split(q1.x), d0 = split(q0.y), d1 = split(q1.y);
+        float4 *o = s.rows + j * 4 * nc + ig;
+        o[0] = make_float4(a0.h, a1.h, a0.l, a1.l);
+        o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
+        o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
+        o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
     }
 }
 
@@ -73,8 +81,8 @@ __global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes
     }
 }
 
-template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int SYNC, int GROUP>
-__global__ void __launch_bounds__(NWARP * 32)
+template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int SYNC, int GROUP, int MINB>
+__global__ void __launch_bounds__(NWARP * 32, MINB)
 mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
                     int row_tiles, int band_tiles) {
     // Grouped tile order: GROUP consecutive row tiles share each band tile,
@@ -94,25 +102,29 @@ constexpr int kGroup = 16;
 constexpr int kWarps = 4;
 
 // Compiled pipeline variants of the mixed kernel (the autotuner picks one).
+// `minb` is the __launch_bounds__ minimum of resident blocks per SM: 0 leaves
+// the register count to the compiler's default heuristic (a minimum of 1
+// would let it take up to 255), 5 caps it at 96 registers.
 struct MixedVariant {
-    int kc, stages, sync;
+    int kc, stages, sync, minb;
     const char *name;
 };
 constexpr MixedVariant kMixedVariants[] = {
-    {128, 2, kSyncBlock, "block-sync, 2 x 128 columns"},
-    {128, 3, kSyncBlock, "block-sync, 3 x 128 columns"},
-    {128, 2, kSyncRing, "mbarrier ring, 2 x 128 columns"},
-    {64, 4, kSyncRing, "mbarrier ring, 4 x 64 columns"},
+    {128, 2, kSyncBlock, 0, "block-sync, 2 x 128 columns"},
+    {128, 3, kSyncBlock, 0, "block-sync, 3 x 128 columns"},
+    {128, 2, kSyncRing, 0, "mbarrier ring, 2 x 128 columns"},
+    {64, 4, kSyncRing, 0, "mbarrier ring, 4 x 64 columns"},
+    {128, 2, kSyncBlock, 5, "block-sync, 2 x 128 columns, 5 blocks/SM"},
 };
 constexpr int kNumMixedVariants = sizeof(kMixedVariants) / sizeof(kMixedVariants[0]);
 
-template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC>
+template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC, int MINB = 0>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
                            int b1, cudaStream_t st) {
     constexpr int BN = kWarps * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
     const size_t smem = sizeof(float4) * NSTAGE * (2 * RG + BN) * KC;
-    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup>;
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup, MINB>;
     // Opt in to the full dynamic size (the default cap is 48 KB including
     // the kernel's static shared memory).
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -131,6 +143,7 @@ cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
         case 0: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, st);
         case 2: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, st);
         case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, st);
+        case 4: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, st);
         default: return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
     }
 }
@@ -139,9 +152,9 @@ cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
 
 static int nwc_for(int nw) { return nw <= 4 ? nw : 8; }
 
-// Rows per block for a frequency chunk: 2 rows x 4 frequencies keeps the df
-// accumulators (RG * NWC * 2 values of 2 floats) within ~100 registers.
-static int mixed_rg(int nwc) { return nwc <= 4 ? 2 : 1; }
+// Rows per block: one row pair of the split planes, the two lanes of the
+// packed df2 arithmetic.
+static int mixed_rg(int) { return 2; }
 
 TileShape mixed_noflag_shape(const Problem &p) {
     const int nwc = nwc_for(p.nw);
@@ -155,7 +168,7 @@ const char *mixed_variant_name(int v) {
 int mixed_default_variant() { return 0; }
 
 size_t mixed_split_bytes(const Problem &p) {
-    return sizeof(float4) * ((size_t)2 * p.ng * p.nc + (size_t)p.nb * p.nc) +
+    return sizeof(float4) * (row_pair_elems(p) + (size_t)p.nb * p.nc) +
            sizeof(float2) * (size_t)p.nb * p.nw;
 }
 
@@ -218,7 +231,7 @@ cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *sp
         case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
         case 3: return launch_mixed_variant<1, 2, 3>(variant, p, part, s, b0, b1, st);
         case 4: return launch_mixed_t<1, 2, 4, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
-        default: return launch_mixed_variant<1, 1, 8>(variant, p, part, s, b0, b1, st);
+        default: return launch_mixed_variant<1, 2, 8>(variant, p, part, s, b0, b1, st);
     }
 }
 

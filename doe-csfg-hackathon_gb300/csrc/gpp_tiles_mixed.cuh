@@ -4,18 +4,29 @@
 #pragma once
 
 #include "gpp_df.cuh"
+#include "gpp_df2.cuh"
 #include "gpp_internal.cuh"
 #include "gpp_tiles_fp64.cuh"
 
 namespace gpp {
 
-// Split planes written by the prep kernels (all float4 = 16 bytes).
+// Split planes written by the prep kernels.  G' rows are stored in pairs
+// (rows 2j and 2j+1; the second repeats row ng-1 when ng is odd) as four
+// float4 planes per pair, so that one 16-byte load yields both rows' values
+// as two aligned register pairs, the operands of the packed f32x2
+// instructions:
+//   rows[j][0][ig] = (wt.re hi of row 2j, hi of row 2j+1, lo of 2j, lo of 2j+1)
+//   rows[j][1][ig] = the same for wt.im
+//   rows[j][2][ig], rows[j][3][ig] = the same for Q.re, Q.im (Q = wt*I_eps, FP64)
 struct SplitPlanes {
-    float4 *rowW;  // [ng][nc]: wt.re hi, lo, wt.im hi, lo
-    float4 *rowQ;  // [ng][nc]: (wt*I_eps).re hi, lo, .im hi, lo
+    float4 *rows;  // [ceil(ng/2)][4][nc]
     float4 *band;  // [nb][nc]: aqsn.re hi, lo, .im hi, lo
     float2 *wx;    // [nb][nw]: wx hi, lo
 };
+// One row of a row pair's plane value: (hi, lo) of row 2j + g.
+__device__ __forceinline__ df pair_lane(const float4 &v, int g) {
+    return g == 0 ? df{v.x, v.z} : df{v.y, v.w};
+}
 
 // The full term in FP64 from the original inputs, for |wdiff| < 1e-3 |wx|.
 static __device__ __noinline__ void pole_term_fp64(const Problem &p, int row, int band, int ig, int iw,
@@ -85,55 +96,60 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
         : "memory");
 }
 
-// The df arithmetic of one ig column for one warp: RNW bands x RG rows x NWC
-// frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into acc.  Terms
-// within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs.
-template <int RNW, int RG, int NWC, int KC>
+// The df arithmetic of one ig column for one warp: RNW bands x the tile's
+// two rows x NWC frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into
+// acc.  Every value is a df2 whose lanes are rows row0 and row0 + 1, so one
+// packed f32x2 instruction advances both rows' terms; the row-pair planes
+// load straight into lane pairs and band values broadcast to both lanes.
+// Re(wdiff) is left unnormalised after its cancelling subtraction; its
+// square keeps the l*l term and the reciprocal is seeded from h + l, which
+// keeps the per-term error near 2^-44 relative.  Terms within 1e-3 |wx| of
+// the pole are recomputed in FP64 from the inputs.
+template <int RNW, int NWC, int KC>
 __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
-                                             const float4 *sb, int il, int ig,
-                                             int row0, int bandw, int band_end, int iw0,
+                                             const float4 *sb, int il, int ig, int row0,
+                                             int bandw, int band_end, int iw0,
                                              const df (&wx)[RNW][NWC],
                                              const float (&pole_thr)[RNW][NWC],
-                                             df (&acc)[RNW][RG][NWC][2]) {
-    df wtr[RG], wti[RG], wti2[RG], qr[RG], qi[RG];
-#pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        const float4 wv = st[g * KC + il];
-        const float4 qv = st[(RG + g) * KC + il];
-        wtr[g] = df{wv.x, wv.y};
-        wti[g] = df{wv.z, wv.w};
-        qr[g] = df{qv.x, qv.y};
-        qi[g] = df{qv.z, qv.w};
-        wti2[g] = df_sqr(wti[g]);
-    }
+                                             df2 (&acc)[RNW][NWC][2]) {
+    const float4 vr = st[il], vi = st[KC + il], vqr = st[2 * KC + il], vqi = st[3 * KC + il];
+    const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)};
+    const df2 wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
+    const df2 qr = {f2(vqr.x, vqr.y), f2(vqr.z, vqr.w)};
+    const df2 qi = {f2(vqi.x, vqi.y), f2(vqi.z, vqi.w)};
+    const df2 wti2 = df2_mul(wti, wti);
 #pragma unroll
     for (int n = 0; n < RNW; ++n) {
         const float4 av = sb[n * KC + il];
-        const df ar = {av.x, av.y}, ai = {av.z, av.w};
+        const df2 ar = df2_bcast(df{av.x, av.y}), ai = df2_bcast(df{av.z, av.w});
+        // A = aqsn * Q (frequency independent)
+        const df2 Ar = df2_sub(df2_mul(ar, qr), df2_mul(ai, qi));
+        const df2 Ai = df2_add(df2_mul(ar, qi), df2_mul(ai, qr));
+        const df2 Ai_wti = df2_mul(Ai, wti);
+        const df2 Ar_wti = df2_mul(Ar, wti);
 #pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            // A = aqsn * Q (frequency independent)
-            const df Ar = df_sub(df_mul(ar, qr[g]), df_mul(ai, qi[g]));
-            const df Ai = df_add(df_mul(ar, qi[g]), df_mul(ai, qr[g]));
-            const df Ai_wti = df_mul(Ai, wti[g]);
-            const df Ar_wti = df_mul(Ar, wti[g]);
+        for (int w = 0; w < NWC; ++w) {
+            const df2 wr = df2_sub(df2_bcast(wx[n][w]), wtr);  // Re(wdiff)
+            const df2 d = df2_add(df2_sqr_full(wr), wti2);    // |wdiff|^2
+            const df2 r = df2_rcp(d);
+            // A conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
+            df2 tre = df2_mul(df2_sub(df2_mul(Ar, wr), Ai_wti), r);
+            df2 tim = df2_mul(df2_add(df2_mul(Ai, wr), Ar_wti), r);
+            const float thr = pole_thr[n][w];
+            if (!(d.h.x >= thr) || !(d.h.y >= thr)) {
 #pragma unroll
-            for (int w = 0; w < NWC; ++w) {
-                const df wr = df_norm(df_sub(wx[n][w], wtr[g]));  // Re(wdiff)
-                const df d = df_add(df_sqr(wr), wti2[g]);         // |wdiff|^2
-                df tre, tim;
-                if (d.h >= pole_thr[n][w]) {
-                    const df r = df_rcp(d);
-                    // A * conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
-                    tre = df_mul(df_sub(df_mul(Ar, wr), Ai_wti), r);
-                    tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), r);
-                } else {
-                    pole_term_fp64(p, min(row0 + g, p.ng - 1), min(bandw + n, band_end - 1), ig,
-                                   min(iw0 + w, p.nw - 1), tre, tim);
+                for (int g = 0; g < 2; ++g) {
+                    if (!((g == 0 ? d.h.x : d.h.y) >= thr)) {
+                        df a, b;
+                        pole_term_fp64(p, min(row0 + g, p.ng - 1), min(bandw + n, band_end - 1),
+                                       ig, min(iw0 + w, p.nw - 1), a, b);
+                        df2_set_lane(tre, g, a);
+                        df2_set_lane(tim, g, b);
+                    }
                 }
-                acc[n][g][w][0] = df_add(acc[n][g][w][0], tre);
-                acc[n][g][w][1] = df_add(acc[n][g][w][1], tim);
             }
+            acc[n][w][0] = df2_add(acc[n][w][0], tre);
+            acc[n][w][1] = df2_add(acc[n][w][1], tim);
         }
     }
 }
@@ -143,11 +159,11 @@ enum : int { kSyncBlock = 0, kSyncRing = 1 };
 // Unoccupied bands, mixed precision.  A block owns RG local G' rows and
 // NWARP * RNW bands; warp w owns bands band0 + w*RNW .. +RNW-1.  The ig range
 // is processed in chunks of KC columns through an NSTAGE-deep shared-memory
-// ring: thread 0 streams each chunk's row planes (wtilde, Q: RG x KC x 16 B
-// each) and band planes (aqsn: NWARP*RNW x KC x 16 B) into a stage with 1-D
-// bulk TMA copies that complete on the stage's "full" mbarrier; each warp
-// reads the rows (one copy serves all warps) and its own bands, lanes on
-// consecutive ig (conflict-free 16-byte LDS).  Two ways to recycle a stage:
+// ring: thread 0 streams each chunk's row-pair planes (wt.re, wt.im, Q.re,
+// Q.im: 4 x KC x 16 B) and band planes (aqsn: NWARP*RNW x KC x 16 B) into a
+// stage with 1-D bulk TMA copies that complete on the stage's "full"
+// mbarrier; each warp reads the rows (one copy serves all warps) and its own
+// bands, lanes on consecutive ig (conflict-free 16-byte LDS).  Two ways to recycle a stage:
 //  * kSyncBlock: one __syncthreads per chunk; the refill of the stage read in
 //    the previous chunk is issued right after it, NSTAGE-1 chunks ahead;
 //  * kSyncRing: each warp arrives on the stage's "empty" mbarrier, and the
@@ -172,6 +188,7 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
     constexpr int STAGE = (2 * RG + BN) * KC;  // float4 per stage
     static_assert(KC % 32 == 0, "chunk must be a multiple of the warp width");
     static_assert(NSTAGE >= 2, "need at least two stages");
+    static_assert(RG == 2, "tiles cover one row pair of the split planes");
     extern __shared__ __align__(128) float4 stage_mem[];
     __shared__ unsigned long long full_bar[NSTAGE], empty_bar[NSTAGE];
     __shared__ int abort_flag;
@@ -194,12 +211,10 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
         float4 *st = stage_mem + (c % NSTAGE) * STAGE;
         unsigned long long *bar = &full_bar[c % NSTAGE];
         mbar_expect_tx(bar, bytes * (2 * RG + BN));
+        // The row pair's four planes (wt.re, wt.im, Q.re, Q.im).
+        const size_t r = (size_t)row_tile * 4 * nc + k0;
 #pragma unroll
-        for (int g = 0; g < RG; ++g) {
-            const size_t r = (size_t)min(row0 + g, p.ng - 1) * nc + k0;
-            bulk_copy_g2s(st + g * KC, s.rowW + r, bytes, bar);
-            bulk_copy_g2s(st + (RG + g) * KC, s.rowQ + r, bytes, bar);
-        }
+        for (int k = 0; k < 4; ++k) bulk_copy_g2s(st + k * KC, s.rows + r + (size_t)k * nc, bytes, bar);
 #pragma unroll
         for (int n = 0; n < BN; ++n) {
             const size_t b = (size_t)min(band0 + n, band_end - 1) * nc + k0;
@@ -237,16 +252,14 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
         }
     }
-    df acc[RNW][RG][NWC][2];
+    df2 acc[RNW][NWC][2];  // lanes: the two rows
 #pragma unroll
     for (int n = 0; n < RNW; ++n)
 #pragma unroll
-        for (int g = 0; g < RG; ++g)
-#pragma unroll
-            for (int w = 0; w < NWC; ++w) {
-                acc[n][g][w][0] = {0.f, 0.f};
-                acc[n][g][w][1] = {0.f, 0.f};
-            }
+        for (int w = 0; w < NWC; ++w) {
+            acc[n][w][0] = {f2(0.f, 0.f), f2(0.f, 0.f)};
+            acc[n][w][1] = {f2(0.f, 0.f), f2(0.f, 0.f)};
+        }
 
     int c_stop = nchunks;  // first chunk thread 0 did not consume
     for (int c = 0; c < nchunks; ++c) {
@@ -274,8 +287,8 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             const int cnt = min(KC, nc - k0);
 #pragma unroll 1
             for (int il = lane; il < cnt; il += 32)
-                mixed_column<RNW, RG, NWC, KC>(p, st, sb, il, k0 + il, row0, bandw, band_end,
-                                               iw0, wx, pole_thr, acc);
+                mixed_column<RNW, NWC, KC>(p, st, sb, il, k0 + il, row0, bandw, band_end, iw0,
+                                           wx, pole_thr, acc);
         }
         if (SYNC == kSyncBlock) {
             __syncthreads();  // every warp is done with stage sidx
@@ -317,7 +330,8 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             for (int w = 0; w < NWC; ++w)
 #pragma unroll
                 for (int ri = 0; ri < 2; ++ri) {
-                    df v = acc[n][g][w][ri];
+                    df v;
+                    v = df2_lane(acc[n][w][ri], g);
 #pragma unroll
                     for (int off = 16; off > 0; off >>= 1) {
                         const df o = {__shfl_down_sync(0xffffffffu, v.h, off),
@@ -371,20 +385,14 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
                                                 const SplitPlanes &s, int row_tile, int band,
                                                 int iw_chunk, long long tile, double *red,
                                                 double *S) {
+    static_assert(RG == 2, "tiles cover one row pair of the split planes");
     constexpr int K = RG * NWC * 4;
     const int row0 = row_tile * RG;
     const int iw0 = iw_chunk * NWC;
     const int nc = p.nc;
     const df kLim2 = df_of(kLimitTwo), kLim1 = df_of(kLimitOne), kT1 = df_of(kTo1);
 
-    const float4 *rw[RG];
-    const float4 *rq[RG];
-#pragma unroll
-    for (int g = 0; g < RG; ++g) {
-        const int r = min(row0 + g, p.ng - 1);
-        rw[g] = s.rowW + (size_t)r * nc;
-        rq[g] = s.rowQ + (size_t)r * nc;
-    }
+    const float4 *rp = s.rows + (size_t)row_tile * 4 * nc;  // this row pair's planes
     const float4 *bp = s.band + (size_t)band * nc;
     df wx[NWC], cwr2[NWC];
     double wx64[NWC], cwr[NWC];
@@ -412,11 +420,12 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
     for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
         const float4 av = __ldg(bp + ig);
         const df ar = {av.x, av.y}, ai = {av.z, av.w};
+        const float4 pwr = __ldg(rp + ig), pwi = __ldg(rp + nc + ig);
+        const float4 pqr = __ldg(rp + 2 * nc + ig), pqi = __ldg(rp + 3 * nc + ig);
 #pragma unroll
         for (int g = 0; g < RG; ++g) {
-            const float4 wv = __ldg(rw[g] + ig);
-            const float4 qv = __ldg(rq[g] + ig);
-            const df wtr = {wv.x, wv.y}, wti = {wv.z, wv.w}, qr = {qv.x, qv.y}, qi = {qv.z, qv.w};
+            const df wtr = pair_lane(pwr, g), wti = pair_lane(pwi, g);
+            const df qr = pair_lane(pqr, g), qi = pair_lane(pqi, g);
             const df wti2 = df_sqr(wti);
             const df awt2 = df_add(df_sqr(wtr), wti2);                         // |wtilde|^2
             df w2r, w2i;                                                          // wtilde^2
