@@ -373,7 +373,7 @@ def main() -> int:
         arrays[k] = host.numpy()
     h2d = int(sum(a.nbytes for a in arrays.values()))
     d2h = 2 * shape.nw * 16
-    e2e_times = []
+    e2e_times, e2e_parts = [], []
     with ops.HostContext() as ctx:
         for i in range(2 + max(5, args.steps // 2)):
             barrier()
@@ -382,6 +382,7 @@ def main() -> int:
             dt = time.perf_counter() - t0
             if i >= 2:
                 e2e_times.append(dt)
+                e2e_parts.append(ctx.last_timing())
     e2e_s = gdist.max_over_ranks(statistics.median(e2e_times), dist, "cuda")
 
     if rank != 0:
@@ -425,7 +426,10 @@ def main() -> int:
             "clocks": clk,
             "e2e": {"value": ws * nterms / e2e_s, "unit": "terms/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
-                    "path": "gpp_sigma_host from pinned host buffers (median of steps)"},
+                    "path": "gpp_sigma_host from pinned host buffers (median of steps)",
+                    "device_ms_median": {k: statistics.median(p[k] for p in e2e_parts)
+                                         for k in ("h2d_ms", "compute_ms", "d2h_ms")},
+                    "wall_ms_all": [round(t * 1e3, 1) for t in e2e_times]},
             "roofline": roofline}
     if fp64_leg:
         line["fp64"] = fp64_leg

@@ -583,6 +583,8 @@ struct gpp_context {
     void *dev = nullptr;
     size_t dev_bytes = 0;
     int device = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // H2D, compute, D2H bounds
+    bool timed = false;
 };
 
 gpp_status gpp_context_create(gpp_context **ctx) {
@@ -590,7 +592,11 @@ gpp_status gpp_context_create(gpp_context **ctx) {
     gpp_context *c = new gpp_context();
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     if (e != cudaSuccess) {
+        for (int i = 0; i < 4; ++i)
+            if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+        if (c->stream) cudaStreamDestroy(c->stream);
         delete c;
         return cuda_fail(e, "gpp_context_create");
     }
@@ -602,6 +608,8 @@ gpp_status gpp_context_destroy(gpp_context *ctx) {
     if (!ctx) return GPP_OK;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->dev) cudaFree(ctx->dev);
+    for (int i = 0; i < 4; ++i)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GPP_OK;
@@ -638,6 +646,8 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
         ctx->dev_bytes = off;
     }
     char *d = static_cast<char *>(ctx->dev);
+    ctx->timed = false;
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
     for (auto &sg : in)
         if (sg.bytes)
             GPP_CUDA_TRY(cudaMemcpyAsync(d + sg.off, sg.src, sg.bytes, cudaMemcpyHostToDevice, ctx->stream),
@@ -658,18 +668,34 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     o.achstemp = dout + 2 * nw;
     o.acht_n1_loc = out->acht_n1_loc ? dout + 2 * nw + 1 : nullptr;
     if (!out->achstemp) o.achstemp = nullptr;
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
     st = gpp_sigma(&q, &o, reinterpret_cast<gpp_stream_t>(ctx->stream));
     if (st != GPP_OK) return st;
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
     const size_t out_bytes = 16 * (2 * nw + 1 + (out->acht_n1_loc ? nb : 0));
     std::vector<gpp_complex> tmp(out_bytes / 16);
     GPP_CUDA_TRY(cudaMemcpyAsync(tmp.data(), dout, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
                  "cudaMemcpyAsync(D2H)");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[3], ctx->stream), "cudaEventRecord");
     st = gpp_wait(reinterpret_cast<gpp_stream_t>(ctx->stream), -1);
     if (st != GPP_OK) return st;
+    ctx->timed = true;
     memcpy(out->achtemp, tmp.data(), 16 * nw);
     memcpy(out->asxtemp, tmp.data() + nw, 16 * nw);
     if (out->achstemp) out->achstemp[0] = tmp[2 * nw];
     if (out->acht_n1_loc) memcpy(out->acht_n1_loc, tmp.data() + 2 * nw + 1, 16 * nb);
+    return GPP_OK;
+}
+
+gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compute_ms,
+                                   float *d2h_ms) {
+    if (!ctx) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx is NULL");
+    if (!ctx->timed) return fail(GPP_ERR_NOT_READY, "no completed gpp_sigma_host call");
+    float *dst[3] = {h2d_ms, compute_ms, d2h_ms};
+    for (int i = 0; i < 3; ++i)
+        if (dst[i])
+            GPP_CUDA_TRY(cudaEventElapsedTime(dst[i], ctx->ev[i], ctx->ev[i + 1]),
+                         "cudaEventElapsedTime");
     return GPP_OK;
 }
 

@@ -40,14 +40,23 @@ SplitPlanes planes(const Problem &p, void *ws) {
     s.rows = static_cast<float4 *>(ws);
     s.band = s.rows + row_pair_elems(p);
     s.wx = reinterpret_cast<float2 *>(s.band + (size_t)p.nb * p.nc);
+    s.masks = reinterpret_cast<unsigned long long *>(s.wx + (size_t)p.nb * p.nw);
     return s;
+}
+
+size_t mask_words(const Problem &p) {
+    return (size_t)((p.ng + 1) / 2) * ((p.nc + kMaskCols - 1) / kMaskCols);
 }
 
 // One thread per (row pair, ig): Q = wtilde * I_eps in FP64 for both rows,
 // then the hi/lo splits interleaved by row (the row-pair plane layout).
+// The same pass sets the row pairs' value-bucket masks: lanes that share a
+// mask word OR their bits together and one of them updates the word (the
+// result does not depend on the order).
 __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s) {
     const size_t nc = (size_t)p.nc;
     const size_t n = (size_t)((p.ng + 1) / 2) * nc;
+    const size_t nmw = (nc + kMaskCols - 1) / kMaskCols;
     for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
         const size_t j = i / nc, ig = i - j * nc;
         const size_t r0 = 2 * j, r1 = min(2 * j + 1, (size_t)p.ng - 1);
@@ -61,6 +70,14 @@ __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes 
         o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
         o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
         o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
+        const unsigned long long bits = bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
+        const unsigned long long word = j * nmw + ig / kMaskCols;
+        const unsigned act = __activemask();
+        const unsigned grp = __match_any_sync(act, word);
+        const unsigned lo = __reduce_or_sync(grp, (unsigned)bits);
+        const unsigned hi = __reduce_or_sync(grp, (unsigned)(bits >> 32));
+        if ((int)(threadIdx.x & 31) == __ffs(grp) - 1)
+            atomicOr(s.masks + word, ((unsigned long long)hi << 32) | lo);
     }
 }
 
@@ -124,7 +141,10 @@ cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPl
     constexpr int BN = kWarps * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
     const size_t smem = sizeof(float4) * NSTAGE * (2 * RG + BN) * KC;
-    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup, MINB>;
+    // The 8-frequency tile holds 64 accumulator registers: keep it at three
+    // resident blocks unless the variant asks for more.
+    constexpr int kMinB = MINB ? MINB : (NWC > 4 ? 3 : 0);
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup, kMinB>;
     // Opt in to the full dynamic size (the default cap is 48 KB including
     // the kernel's static shared memory).
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -169,7 +189,7 @@ int mixed_default_variant() { return 0; }
 
 size_t mixed_split_bytes(const Problem &p) {
     return sizeof(float4) * (row_pair_elems(p) + (size_t)p.nb * p.nc) +
-           sizeof(float2) * (size_t)p.nb * p.nw;
+           sizeof(float2) * (size_t)p.nb * p.nw + sizeof(unsigned long long) * mask_words(p);
 }
 
 SplitPlanes split_planes_at(const Problem &p, void *split_ws) { return planes(p, split_ws); }
@@ -180,6 +200,8 @@ cudaError_t launch_split(const Problem &p, void *split_ws, int b0, int b1, cudaS
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = sms > 0 ? sms * 8 : 1024;
+    cudaError_t e = cudaMemsetAsync(s.masks, 0, sizeof(unsigned long long) * mask_words(p), st);
+    if (e != cudaSuccess) return e;
     split_rows_kernel<<<blocks, 256, 0, st>>>(p, s);
     split_bands_kernel<<<blocks, 256, 0, st>>>(p, s, b0, b1);
     count_launch(2);

@@ -3,6 +3,8 @@
 // the one-state kernel (gpp_mixed.cu) and the persistent batched kernels.
 #pragma once
 
+#include <cstring>
+
 #include "gpp_df.cuh"
 #include "gpp_df2.cuh"
 #include "gpp_internal.cuh"
@@ -18,11 +20,45 @@ namespace gpp {
 //   rows[j][0][ig] = (wt.re hi of row 2j, hi of row 2j+1, lo of 2j, lo of 2j+1)
 //   rows[j][1][ig] = the same for wt.im
 //   rows[j][2][ig], rows[j][3][ig] = the same for Q.re, Q.im (Q = wt*I_eps, FP64)
+// masks[j][k] has a bit for every value bucket (below) that Re(wtilde) hi of
+// rows 2j, 2j+1 takes in columns 64k .. 64k+63, written by the row split.
+// A warp skips the per-term pole test for a chunk when none of the chunk's
+// buckets can hold a wtilde within the pole distance of its wx values.
 struct SplitPlanes {
-    float4 *rows;  // [ceil(ng/2)][4][nc]
-    float4 *band;  // [nb][nc]: aqsn.re hi, lo, .im hi, lo
-    float2 *wx;    // [nb][nw]: wx hi, lo
+    float4 *rows;                 // [ceil(ng/2)][4][nc]
+    float4 *band;                 // [nb][nc]: aqsn.re hi, lo, .im hi, lo
+    float2 *wx;                   // [nb][nw]: wx hi, lo
+    unsigned long long *masks;    // [ceil(ng/2)][ceil(nc/64)], zeroed before the split
 };
+constexpr int kMaskCols = 64;
+// Monotonic map of floats onto unsigned integers (integer order = float
+// order).
+__host__ __device__ __forceinline__ unsigned float_key(float f) {
+    unsigned u;
+    memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+// Value bucket: the top 11 bits of the key (sign, exponent, two mantissa
+// bits, in value order), hashed onto one of 64 mask bits.  Shared bits only
+// cost a needless test, never a missed one.
+__host__ __device__ __forceinline__ unsigned bucket_code(float f) { return float_key(f) >> 21; }
+__host__ __device__ __forceinline__ unsigned long long bucket_bit(unsigned code) {
+    return 1ull << ((code ^ (code >> 6)) & 63);
+}
+// Mask bits of every bucket a wtilde within the FP64 pole distance of x
+// (|wdiff|^2 < 1e-6 x^2, so |x - Re(wtilde)| < 1e-3 |x|) can fall into, with
+// a margin far above the float rounding of both sides; all bits for NaN.
+__host__ __device__ __forceinline__ unsigned long long pole_buckets(float x) {
+    const float rad = 1.01e-3f * fabsf(x) + 1e-30f;
+    const float lo = x - rad, hi = x + rad;
+    if (!(lo <= hi)) return ~0ull;
+    const unsigned c0 = bucket_code(lo), c1 = bucket_code(hi);
+    if (c1 - c0 >= 64) return ~0ull;
+    unsigned long long m = 0;
+    for (unsigned c = c0; c <= c1; ++c) m |= bucket_bit(c);
+    return m;
+}
+
 // One row of a row pair's plane value: (hi, lo) of row 2j + g.
 __device__ __forceinline__ df pair_lane(const float4 &v, int g) {
     return g == 0 ? df{v.x, v.z} : df{v.y, v.w};
@@ -96,6 +132,26 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
         : "memory");
 }
 
+// The lanes of a term pair that lie near the pole (d.h < thr), recomputed in
+// FP64 from the inputs.  Out of line and returning whole pairs by value, so
+// the rare per-lane update does not split the pairs' registers in the hot
+// loop.
+struct TermPair {
+    df2 re, im;
+};
+static __device__ __noinline__ TermPair pole_pair(const Problem &p, df2 d, float thr, int row0,
+                                                  int band, int ig, int iw, TermPair t) {
+    for (int g = 0; g < 2; ++g) {
+        if (!((g == 0 ? d.h.x : d.h.y) >= thr)) {
+            df x, y;
+            pole_term_fp64(p, min(row0 + g, p.ng - 1), band, ig, iw, x, y);
+            df2_set_lane(t.re, g, x);
+            df2_set_lane(t.im, g, y);
+        }
+    }
+    return t;
+}
+
 // The df arithmetic of one ig column for one warp: RNW bands x the tile's
 // two rows x NWC frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into
 // acc.  Every value is a df2 whose lanes are rows row0 and row0 + 1, so one
@@ -103,9 +159,11 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsign
 // load straight into lane pairs and band values broadcast to both lanes.
 // Re(wdiff) is left unnormalised after its cancelling subtraction; its
 // square keeps the l*l term and the reciprocal is seeded from h + l, which
-// keeps the per-term error near 2^-44 relative.  Terms within 1e-3 |wx| of
-// the pole are recomputed in FP64 from the inputs.
-template <int RNW, int NWC, int KC>
+// keeps the per-term error near 2^-44 relative.  With CHECK, terms within
+// 1e-3 |wx| of the pole are recomputed in FP64 from the inputs; tiles call
+// the CHECK = false form only when no wtilde can come that near any of the
+// warp's wx values.
+template <int RNW, int NWC, int KC, bool CHECK>
 __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
                                              const float4 *sb, int il, int ig, int row0,
                                              int bandw, int band_end, int iw0,
@@ -135,17 +193,13 @@ __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
             // A conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
             df2 tre = df2_mul(df2_sub(df2_mul(Ar, wr), Ai_wti), r);
             df2 tim = df2_mul(df2_add(df2_mul(Ai, wr), Ar_wti), r);
-            const float thr = pole_thr[n][w];
-            if (!(d.h.x >= thr) || !(d.h.y >= thr)) {
-#pragma unroll
-                for (int g = 0; g < 2; ++g) {
-                    if (!((g == 0 ? d.h.x : d.h.y) >= thr)) {
-                        df a, b;
-                        pole_term_fp64(p, min(row0 + g, p.ng - 1), min(bandw + n, band_end - 1),
-                                       ig, min(iw0 + w, p.nw - 1), a, b);
-                        df2_set_lane(tre, g, a);
-                        df2_set_lane(tim, g, b);
-                    }
+            if (CHECK) {
+                const float thr = pole_thr[n][w];
+                if (!(d.h.x >= thr) || !(d.h.y >= thr)) {
+                    const TermPair t = pole_pair(p, d, thr, row0, min(bandw + n, band_end - 1),
+                                                 ig, min(iw0 + w, p.nw - 1), TermPair{tre, tim});
+                    tre = t.re;
+                    tim = t.im;
                 }
             }
             acc[n][w][0] = df2_add(acc[n][w][0], tre);
@@ -242,6 +296,9 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
 
     df wx[RNW][NWC];
     float pole_thr[RNW][NWC];
+    unsigned long long pole_mask = 0;  // value buckets of a possible pole term
+    const unsigned long long *mask_row =
+        s.masks + (size_t)row_tile * ((nc + kMaskCols - 1) / kMaskCols);
 #pragma unroll
     for (int n = 0; n < RNW; ++n) {
         const int b = min(bandw + n, band_end - 1);
@@ -250,6 +307,7 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
             wx[n][w] = {x.x, x.y};
             pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
+            pole_mask |= pole_buckets(x.x);
         }
     }
     df2 acc[RNW][NWC][2];  // lanes: the two rows
@@ -278,6 +336,10 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             }
         }
         if (SYNC == kSyncRing && warp == 0) __syncwarp();  // warp 0 waits for its producer lane
+        // Value buckets of this chunk's wtilde (read before the wait).
+        unsigned long long chunk_mask = 0;
+        for (int k = (c * KC) / kMaskCols; k <= (min(c * KC + KC, nc) - 1) / kMaskCols; ++k)
+            chunk_mask |= __ldg(mask_row + k);
         const int sidx = c % NSTAGE;
         const bool ok = mbar_wait(&full_bar[sidx], (unsigned)((c / NSTAGE) & 1), abort);
         if (ok) {
@@ -285,10 +347,17 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             const float4 *sb = st + (2 * RG + warp * RNW) * KC;  // this warp's bands
             const int k0 = c * KC;
             const int cnt = min(KC, nc - k0);
+            if (chunk_mask & pole_mask) {
 #pragma unroll 1
-            for (int il = lane; il < cnt; il += 32)
-                mixed_column<RNW, NWC, KC>(p, st, sb, il, k0 + il, row0, bandw, band_end, iw0,
-                                           wx, pole_thr, acc);
+                for (int il = lane; il < cnt; il += 32)
+                    mixed_column<RNW, NWC, KC, true>(p, st, sb, il, k0 + il, row0, bandw,
+                                                     band_end, iw0, wx, pole_thr, acc);
+            } else {
+#pragma unroll 1
+                for (int il = lane; il < cnt; il += 32)
+                    mixed_column<RNW, NWC, KC, false>(p, st, sb, il, k0 + il, row0, bandw,
+                                                      band_end, iw0, wx, pole_thr, acc);
+            }
         }
         if (SYNC == kSyncBlock) {
             __syncthreads();  // every warp is done with stage sidx

@@ -67,6 +67,8 @@ _SIGS = {
     "gpp_enable_kernel_timing": (_i, [_i]),
     "gpp_last_kernel_ms": (_i, [C.POINTER(C.c_float)]),
     "gpp_probe_fma_peaks": (_i, [C.POINTER(_d), C.POINTER(_d)]),
+    "gpp_context_last_timing": (_i, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                     C.POINTER(C.c_float)]),
 }
 
 _lib = None

@@ -289,3 +289,11 @@ class HostContext:
             o.achstemp = res["achstemp"].ctypes.data
         capi.check(self._lib.gpp_sigma_host(self.handle, C.byref(p), C.byref(o)), "gpp_sigma_host")
         return res
+
+    def last_timing(self) -> dict:
+        """Device-side milliseconds of the last sigma call: H2D copies,
+        gpp_sigma, D2H copy (CUDA events on the context's stream)."""
+        t = [C.c_float() for _ in range(3)]
+        capi.check(self._lib.gpp_context_last_timing(self.handle, *[C.byref(x) for x in t]),
+                   "gpp_context_last_timing")
+        return {"h2d_ms": t[0].value, "compute_ms": t[1].value, "d2h_ms": t[2].value}

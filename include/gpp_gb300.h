@@ -169,6 +169,11 @@ typedef struct gpp_context gpp_context;
 gpp_status gpp_context_create(gpp_context **ctx);
 gpp_status gpp_context_destroy(gpp_context *ctx);
 gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gpp_outputs *out);
+/* Where the last gpp_sigma_host call on `ctx` spent its device time, from
+ * CUDA events on the context's stream: host-to-device copies, gpp_sigma,
+ * device-to-host copy (milliseconds; any pointer may be NULL). */
+gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compute_ms,
+                                   float *d2h_ms);
 
 /* No counterpart in the reference.  gpp_sigma for callers that cannot
  * allocate device memory -- applications that have handed the GPU's memory

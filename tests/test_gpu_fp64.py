@@ -151,8 +151,12 @@ def test_host_path_equals_device_path():
     arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
                                            "vcoul", "inv_igp_index", "indinv", "wx_array")}
     with o.HostContext() as ctx:
+        with pytest.raises(capi.GppError):
+            ctx.last_timing()  # nothing timed yet
         host = ctx.sigma(arrays, inp.shape, "fp64", acht_n1=True, achstemp=True)
         host2 = ctx.sigma(arrays, inp.shape, "fp64", acht_n1=True, achstemp=True)
+        t = ctx.last_timing()
+    assert t["h2d_ms"] > 0 and t["compute_ms"] > 0 and t["d2h_ms"] >= 0
     for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
         np.testing.assert_array_equal(host[k], getattr(dev, k).cpu().numpy())
         np.testing.assert_array_equal(host[k], host2[k])

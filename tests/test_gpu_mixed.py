@@ -101,3 +101,27 @@ def test_every_pipeline_variant_gives_the_same_bits_and_autotune_picks_one():
         assert 0 <= best < len(names)
     finally:
         o.set_variant(3, -1)
+
+
+@pytest.mark.parametrize("semantics", ["complex_seq", "kerseq"])
+def test_terms_at_the_pole_take_the_fp64_path(semantics):
+    """wtilde placed 1e-9 from the wx of bands far outside wtilde's usual
+    range (also widening that range): float-float arithmetic would lose ~6
+    digits on these terms, so the result only matches FP64 if every one of
+    them is routed to the FP64 pole path."""
+    o = ops()
+    shape = W.Shape(24, 2, 2048, 40, 3)
+    inp = W.make_inputs(shape, 31)
+    wt = inp.wtilde_array.copy()
+    rng = np.random.default_rng(5)
+    for k in range(60):
+        row, ig = rng.integers(shape.ngpown), rng.integers(shape.ncouls)
+        band, iw = rng.integers(shape.nvband, shape.number_bands), rng.integers(shape.nw)
+        wt[row, ig] = complex(inp.wx_array[band, iw] + 1e-9, 1e-12)
+    inp.wtilde_array = wt
+    d = o.DeviceInputs.from_host(inp)
+    a = o.sigma(d, "fp64", semantics)
+    b = o.sigma(d, "mixed", semantics)
+    o.wait()
+    assert rel_err(b.achtemp.cpu().numpy(), a.achtemp.cpu().numpy()) <= MIXED_TOL
+    assert rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy()) <= MIXED_TOL
