@@ -8,6 +8,7 @@
 #include <string>
 #include <thread>
 #include <vector>
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 
@@ -237,8 +238,19 @@ gpp_status side_stream(int dev, SideStream **out) {
 // Runs the bands [b0, b1) of problem p: occupied bands (< nv) through the
 // flag kernel, the rest through the FP64 or mixed unoccupied kernel, then
 // reduces all block partials in a fixed order into the outputs.
+// Row pieces of a call whose G' rows arrive on the device in parts (the
+// host path): piece k covers row pairs [pair[k], pair[k+1]) and its kernels
+// start once ready[k] has fired.  The partial sums land in the same slots
+// as one launch over all rows, so the result does not depend on the pieces.
+constexpr int kMaxRowPieces = 16;
+struct RowPieces {
+    int n = 0;
+    int pair[kMaxRowPieces + 1] = {};
+    cudaEvent_t ready[kMaxRowPieces] = {};
+};
+
 gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutSpec &o,
-                     bool do_main, cudaStream_t s) {
+                     bool do_main, cudaStream_t s, const RowPieces *pieces = nullptr) {
     int dev = 0;
     int *err = nullptr;
     gpp_status st = device_setup(&dev, &err);
@@ -295,30 +307,43 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         e = cudaMemsetAsync(part.n1, 0, sizeof(double2) * (size_t)(n1_seg * p.nb), s);
     }
     if (e == cudaSuccess && mixed)  // float-float planes of every band the call touches
-        e = launch_split(p, w + o_split, has_flag ? fb0 : nb0, has_noflag ? nb1 : fb1, s);
+        e = launch_split_bands(p, w + o_split, has_flag ? fb0 : nb0, has_noflag ? nb1 : fb1, s);
     SideStream *side = nullptr;
-    const bool overlap = mixed && has_flag && has_noflag && overlap_occupied();
+    const bool overlap = mixed && has_flag && has_noflag && overlap_occupied() && !pieces;
+    RowPieces whole;
+    whole.n = 1;
+    whole.pair[0] = 0;
+    whole.pair[1] = (p.ng + 1) / 2;
+    const RowPieces &pc = pieces ? *pieces : whole;
     if (overlap) {
         st = side_stream(dev, &side);
         if (st != GPP_OK) {
             cudaFreeAsync(ws, s);
             return st;
         }
-        if (e == cudaSuccess) e = cudaEventRecord(side->fork, s);
     }
-    if (e == cudaSuccess && has_flag && !overlap) {
-        part.ach_tile0 = 0;
-        e = mixed ? launch_flag_mixed(p, part, w + o_split, s) : launch_flag_fp64(p, part, s);
-    }
-    if (e == cudaSuccess && has_noflag) {
-        part.ach_tile0 = (int)tiles_f;
-        if (t_timing && t_ev0) cudaEventRecord(t_ev0, s);
-        e = mixed ? launch_mixed_noflag(p, part, w + o_split, nb0, nb1, s,
-                                        mixed_variant_for(dev, p.nw))
-                  : launch_noflag_fp64(p, part, nb0, nb1, s);
-        if (t_timing && t_ev1) {
-            cudaEventRecord(t_ev1, s);
-            t_timed = true;
+    const int variant = mixed ? mixed_variant_for(dev, p.nw) : 0;
+    for (int k = 0; k < pc.n && e == cudaSuccess; ++k) {
+        RowTiles rt;
+        rt.begin = pc.pair[k];
+        rt.end = pc.pair[k + 1];
+        if (pieces) e = cudaStreamWaitEvent(s, pc.ready[k], 0);
+        if (e == cudaSuccess && mixed) e = launch_split_rows(p, w + o_split, rt, s);
+        if (e == cudaSuccess && overlap) e = cudaEventRecord(side->fork, s);  // planes written
+        if (e == cudaSuccess && has_flag && !overlap) {
+            part.ach_tile0 = 0;
+            e = mixed ? launch_flag_mixed(p, part, w + o_split, s, rt)
+                      : launch_flag_fp64(p, part, s, rt);
+        }
+        if (e == cudaSuccess && has_noflag) {
+            part.ach_tile0 = (int)tiles_f;
+            if (k == 0 && t_timing && t_ev0) cudaEventRecord(t_ev0, s);
+            e = mixed ? launch_mixed_noflag(p, part, w + o_split, nb0, nb1, s, variant, rt)
+                      : launch_noflag_fp64(p, part, nb0, nb1, s, rt);
+            if (k == pc.n - 1 && t_timing && t_ev1) {
+                cudaEventRecord(t_ev1, s);
+                t_timed = true;
+            }
         }
     }
     if (e == cudaSuccess && overlap) {
@@ -381,7 +406,12 @@ gpp_status gpp_set_stream(gpp_stream_t stream) {
 }
 gpp_stream_t gpp_get_stream(void) { return reinterpret_cast<gpp_stream_t>(t_compat_stream); }
 
-gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_stream_t stream) {
+}  // extern "C"
+
+namespace {
+// gpp_sigma, optionally over G' rows that reach the device in pieces.
+gpp_status sigma_impl(const gpp_problem *problem, const gpp_outputs *out, cudaStream_t s,
+                      const RowPieces *pieces) {
     gpp_status st = validate(problem);
     if (st != GPP_OK) return st;
     if (!out || !out->achtemp || !out->asxtemp)
@@ -389,7 +419,6 @@ gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_str
     if (out->acht_n1_loc && problem->nw < 3)
         return fail(GPP_ERR_INVALID_ARGUMENT, "acht_n1_loc needs nw >= 3 (it sums the iw = 2 column)");
     Problem p = to_problem(*problem);
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     OutSpec o;
     o.ach = reinterpret_cast<double2 *>(out->achtemp);
     o.asx = reinterpret_cast<double2 *>(out->asxtemp);
@@ -404,7 +433,14 @@ gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_str
         cudaError_t e = cudaMemsetAsync(o.achs, 0, sizeof(double2), s);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(achstemp)");
     }
-    return run_sigma(p, 0, p.nb, problem->precision, o, true, s);
+    return run_sigma(p, 0, p.nb, problem->precision, o, true, s, pieces);
+}
+}  // namespace
+
+extern "C" {
+
+gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_stream_t stream) {
+    return sigma_impl(problem, out, reinterpret_cast<cudaStream_t>(stream), nullptr);
 }
 
 gpp_status gpp_kernel_gpu(const gpp_complex *wtilde_array, const gpp_complex *aqsntemp,
@@ -578,26 +614,49 @@ gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms) {
 
 // ---------------------------------------------------------------------------
 // Host-buffer path: a context owns device copies of the inputs and outputs.
+// Input copies run on their own stream in pieces -- the band arrays first,
+// then the G' rows in row-pair ranges -- and the kernels of each piece start
+// as soon as its rows have landed, so the copies overlap the computation.
 struct gpp_context {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // kernels and the result copy
+    cudaStream_t copy = nullptr;    // input copies
     void *dev = nullptr;
     size_t dev_bytes = 0;
     int device = 0;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // H2D, compute, D2H bounds
+    // Copy start, copy end, compute start, compute end, result copy end.
+    cudaEvent_t ev[5] = {};
+    cudaEvent_t bands_ready = nullptr, done = nullptr;
+    cudaEvent_t ready[kMaxRowPieces] = {};
     bool timed = false;
 };
+
+constexpr int kHostRowPieces = 8;
+
+static void context_release(gpp_context *c) {
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->ready)
+        if (e) cudaEventDestroy(e);
+    if (c->bands_ready) cudaEventDestroy(c->bands_ready);
+    if (c->done) cudaEventDestroy(c->done);
+    if (c->copy) cudaStreamDestroy(c->copy);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
 
 gpp_status gpp_context_create(gpp_context **ctx) {
     if (!ctx) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx is NULL");
     gpp_context *c = new gpp_context();
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    for (int i = 0; i < kMaxRowPieces && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&c->ready[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->bands_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
     if (e != cudaSuccess) {
-        for (int i = 0; i < 4; ++i)
-            if (c->ev[i]) cudaEventDestroy(c->ev[i]);
-        if (c->stream) cudaStreamDestroy(c->stream);
-        delete c;
+        context_release(c);
         return cuda_fail(e, "gpp_context_create");
     }
     *ctx = c;
@@ -606,12 +665,10 @@ gpp_status gpp_context_create(gpp_context **ctx) {
 
 gpp_status gpp_context_destroy(gpp_context *ctx) {
     if (!ctx) return GPP_OK;
+    if (ctx->copy) cudaStreamSynchronize(ctx->copy);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->dev) cudaFree(ctx->dev);
-    for (int i = 0; i < 4; ++i)
-        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    context_release(ctx);
     return GPP_OK;
 }
 
@@ -626,6 +683,7 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
                  nw = (size_t)h.nw;
     const size_t wx_n = h.wx_stride ? nb * (size_t)h.wx_stride : nw;
     struct Seg { const void *src; size_t bytes; size_t off; };
+    enum { kAqsm, kAqsn, kIeps, kWt, kVcoul, kInvIgp, kIndinv, kWx };
     std::vector<Seg> in = {
         {h.aqsmtemp, nb * nc * 16, 0}, {h.aqsntemp, nb * nc * 16, 0},
         {h.I_eps_array, ng * nc * 16, 0}, {h.wtilde_array, ng * nc * 16, 0},
@@ -637,6 +695,7 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     off = align_up(off + 16 * (2 * nw + (out->acht_n1_loc ? nb : 0) + 1));
     if (off > ctx->dev_bytes) {
         if (ctx->dev) {
+            cudaStreamSynchronize(ctx->copy);
             cudaStreamSynchronize(ctx->stream);
             cudaFree(ctx->dev);
             ctx->dev = nullptr;
@@ -647,20 +706,41 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     }
     char *d = static_cast<char *>(ctx->dev);
     ctx->timed = false;
-    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[0], ctx->stream), "cudaEventRecord");
-    for (auto &sg : in)
-        if (sg.bytes)
-            GPP_CUDA_TRY(cudaMemcpyAsync(d + sg.off, sg.src, sg.bytes, cudaMemcpyHostToDevice, ctx->stream),
-                         "cudaMemcpyAsync(H2D)");
+    auto h2d = [&](int k, size_t from, size_t bytes) {
+        return cudaMemcpyAsync(d + in[k].off + from, static_cast<const char *>(in[k].src) + from,
+                               bytes, cudaMemcpyHostToDevice, ctx->copy);
+    };
+    // Copies may only overwrite the buffers once the previous call is done.
+    GPP_CUDA_TRY(cudaStreamWaitEvent(ctx->copy, ctx->done, 0), "cudaStreamWaitEvent");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[0], ctx->copy), "cudaEventRecord");
+    for (int k : {kVcoul, kInvIgp, kIndinv, kWx, kAqsm, kAqsn})
+        if (in[k].bytes) GPP_CUDA_TRY(h2d(k, 0, in[k].bytes), "cudaMemcpyAsync(H2D)");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->bands_ready, ctx->copy), "cudaEventRecord");
+    RowPieces pieces;
+    const int pairs = (int)((ng + 1) / 2);
+    pieces.n = pairs < kHostRowPieces ? (pairs > 0 ? pairs : 1) : kHostRowPieces;
+    for (int k = 0; k <= pieces.n; ++k) pieces.pair[k] = (int)((long long)pairs * k / pieces.n);
+    for (int k = 0; k < pieces.n; ++k) {
+        const size_t r0 = 2 * (size_t)pieces.pair[k];
+        const size_t r1 = std::min(2 * (size_t)pieces.pair[k + 1], ng);
+        if (r1 > r0) {
+            GPP_CUDA_TRY(h2d(kWt, r0 * nc * 16, (r1 - r0) * nc * 16), "cudaMemcpyAsync(H2D)");
+            GPP_CUDA_TRY(h2d(kIeps, r0 * nc * 16, (r1 - r0) * nc * 16), "cudaMemcpyAsync(H2D)");
+        }
+        pieces.ready[k] = ctx->ready[k];
+        GPP_CUDA_TRY(cudaEventRecord(ctx->ready[k], ctx->copy), "cudaEventRecord");
+    }
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[1], ctx->copy), "cudaEventRecord");
+
     gpp_problem q = h;
-    q.aqsmtemp = reinterpret_cast<const gpp_complex *>(d + in[0].off);
-    q.aqsntemp = reinterpret_cast<const gpp_complex *>(d + in[1].off);
-    q.I_eps_array = reinterpret_cast<const gpp_complex *>(d + in[2].off);
-    q.wtilde_array = reinterpret_cast<const gpp_complex *>(d + in[3].off);
-    q.vcoul = reinterpret_cast<const double *>(d + in[4].off);
-    q.inv_igp_index = reinterpret_cast<const int *>(d + in[5].off);
-    q.indinv = h.indinv ? reinterpret_cast<const int *>(d + in[6].off) : nullptr;
-    q.wx_array = reinterpret_cast<const double *>(d + in[7].off);
+    q.aqsmtemp = reinterpret_cast<const gpp_complex *>(d + in[kAqsm].off);
+    q.aqsntemp = reinterpret_cast<const gpp_complex *>(d + in[kAqsn].off);
+    q.I_eps_array = reinterpret_cast<const gpp_complex *>(d + in[kIeps].off);
+    q.wtilde_array = reinterpret_cast<const gpp_complex *>(d + in[kWt].off);
+    q.vcoul = reinterpret_cast<const double *>(d + in[kVcoul].off);
+    q.inv_igp_index = reinterpret_cast<const int *>(d + in[kInvIgp].off);
+    q.indinv = h.indinv ? reinterpret_cast<const int *>(d + in[kIndinv].off) : nullptr;
+    q.wx_array = reinterpret_cast<const double *>(d + in[kWx].off);
     gpp_complex *dout = reinterpret_cast<gpp_complex *>(d + o_out);
     gpp_outputs o{};
     o.achtemp = dout;
@@ -668,15 +748,24 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     o.achstemp = dout + 2 * nw;
     o.acht_n1_loc = out->acht_n1_loc ? dout + 2 * nw + 1 : nullptr;
     if (!out->achstemp) o.achstemp = nullptr;
-    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[1], ctx->stream), "cudaEventRecord");
-    st = gpp_sigma(&q, &o, reinterpret_cast<gpp_stream_t>(ctx->stream));
-    if (st != GPP_OK) return st;
+    GPP_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, ctx->bands_ready, 0), "cudaStreamWaitEvent");
     GPP_CUDA_TRY(cudaEventRecord(ctx->ev[2], ctx->stream), "cudaEventRecord");
+    st = sigma_impl(&q, &o, ctx->stream, &pieces);
+    if (st == GPP_OK) {
+        // The kernels waited on every piece; make the ordering explicit for
+        // the zero-row case too.
+        cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev[1], 0);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamWaitEvent");
+    }
+    cudaEventRecord(ctx->done, ctx->stream);
+    if (st != GPP_OK) return st;
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[3], ctx->stream), "cudaEventRecord");
     const size_t out_bytes = 16 * (2 * nw + 1 + (out->acht_n1_loc ? nb : 0));
     std::vector<gpp_complex> tmp(out_bytes / 16);
     GPP_CUDA_TRY(cudaMemcpyAsync(tmp.data(), dout, out_bytes, cudaMemcpyDeviceToHost, ctx->stream),
                  "cudaMemcpyAsync(D2H)");
-    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[3], ctx->stream), "cudaEventRecord");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->ev[4], ctx->stream), "cudaEventRecord");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->done, ctx->stream), "cudaEventRecord");
     st = gpp_wait(reinterpret_cast<gpp_stream_t>(ctx->stream), -1);
     if (st != GPP_OK) return st;
     ctx->timed = true;
@@ -691,11 +780,10 @@ gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compu
                                    float *d2h_ms) {
     if (!ctx) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx is NULL");
     if (!ctx->timed) return fail(GPP_ERR_NOT_READY, "no completed gpp_sigma_host call");
-    float *dst[3] = {h2d_ms, compute_ms, d2h_ms};
-    for (int i = 0; i < 3; ++i)
-        if (dst[i])
-            GPP_CUDA_TRY(cudaEventElapsedTime(dst[i], ctx->ev[i], ctx->ev[i + 1]),
-                         "cudaEventElapsedTime");
+    if (h2d_ms) GPP_CUDA_TRY(cudaEventElapsedTime(h2d_ms, ctx->ev[0], ctx->ev[1]), "cudaEventElapsedTime");
+    if (compute_ms)
+        GPP_CUDA_TRY(cudaEventElapsedTime(compute_ms, ctx->ev[2], ctx->ev[3]), "cudaEventElapsedTime");
+    if (d2h_ms) GPP_CUDA_TRY(cudaEventElapsedTime(d2h_ms, ctx->ev[3], ctx->ev[4]), "cudaEventElapsedTime");
     return GPP_OK;
 }
 

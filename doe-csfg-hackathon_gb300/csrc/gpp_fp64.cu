@@ -17,22 +17,26 @@ namespace {
 
 template <int RN, int RG, int NWC, int THREADS>
 __global__ void __launch_bounds__(THREADS)
-noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end) {
+noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end, int row_tile0,
+                   int row_tiles) {
     constexpr int K = RN * RG * NWC * 2;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    noflag_fp64_tile<RN, RG, NWC, THREADS>(p, part, band_begin, band_end, blockIdx.x, blockIdx.y,
-                                           blockIdx.z, (long long)blockIdx.y * gridDim.x + blockIdx.x,
+    const int row_tile = row_tile0 + blockIdx.x;
+    noflag_fp64_tile<RN, RG, NWC, THREADS>(p, part, band_begin, band_end, row_tile, blockIdx.y,
+                                           blockIdx.z, (long long)blockIdx.y * row_tiles + row_tile,
                                            red, S);
 }
 
 template <int RG, int NWC, int THREADS, int SEM>
-__global__ void __launch_bounds__(THREADS) flag_fp64_kernel(Problem p, Partials part) {
+__global__ void __launch_bounds__(THREADS)
+flag_fp64_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
     constexpr int K = RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    flag_fp64_tile<RG, NWC, THREADS, SEM>(p, part, blockIdx.x, blockIdx.y, blockIdx.z,
-                                          (long long)blockIdx.y * gridDim.x + blockIdx.x, red, S);
+    const int row_tile = row_tile0 + blockIdx.x;
+    flag_fp64_tile<RG, NWC, THREADS, SEM>(p, part, row_tile, blockIdx.y, blockIdx.z,
+                                          (long long)blockIdx.y * row_tiles + row_tile, red, S);
 }
 
 // Static term of reduce_achstemp (gppComplex_seq.cpp:66-101): one thread per
@@ -89,21 +93,30 @@ reduce_kernel(const double2 *src, long long stride, int len, ReduceOut out) {
 }
 
 template <int RN, int RG, int NWC, int THREADS>
-cudaError_t launch_noflag_t(const Problem &p, const Partials &part, int b0, int b1,
+cudaError_t launch_noflag_t(const Problem &p, const Partials &part, int b0, int b1, RowTiles rt,
                             cudaStream_t s) {
-    dim3 grid(ceil_div(p.ng, RG), ceil_div(b1 - b0, RN), ceil_div(p.nw, NWC));
-    noflag_fp64_kernel<RN, RG, NWC, THREADS><<<grid, THREADS, 0, s>>>(p, part, b0, b1);
+    const int row_tiles = ceil_div(p.ng, RG);
+    const RowTiles r = rt.clip(row_tiles);
+    if (r.end <= r.begin) return cudaSuccess;
+    dim3 grid(r.end - r.begin, ceil_div(b1 - b0, RN), ceil_div(p.nw, NWC));
+    noflag_fp64_kernel<RN, RG, NWC, THREADS><<<grid, THREADS, 0, s>>>(p, part, b0, b1, r.begin,
+                                                                       row_tiles);
     count_launch();
     return cudaGetLastError();
 }
 
 template <int RG, int NWC, int THREADS>
-cudaError_t launch_flag_t(const Problem &p, const Partials &part, cudaStream_t s) {
-    dim3 grid(ceil_div(p.ng, RG), p.nv, ceil_div(p.nw, NWC));
+cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, cudaStream_t s) {
+    const int row_tiles = ceil_div(p.ng, RG);
+    const RowTiles r = rt.clip(row_tiles);
+    if (r.end <= r.begin) return cudaSuccess;
+    dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
     if (p.semantics == kSemKerSeq)
-        flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(p, part);
+        flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(p, part, r.begin,
+                                                                                row_tiles);
     else
-        flag_fp64_kernel<RG, NWC, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(p, part);
+        flag_fp64_kernel<RG, NWC, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(
+            p, part, r.begin, row_tiles);
     count_launch();
     return cudaGetLastError();
 }
@@ -122,25 +135,25 @@ TileShape fp64_noflag_shape(const Problem &p) {
 TileShape flag_shape(const Problem &p) { return TileShape{1, 2, nwc_for(p.nw), 128}; }
 
 cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int b0, int b1,
-                               cudaStream_t s) {
+                               cudaStream_t s, RowTiles rt) {
     if (b1 <= b0 || p.ng == 0) return cudaSuccess;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_noflag_t<4, 2, 1, 128>(p, part, b0, b1, s);
-        case 2: return launch_noflag_t<4, 2, 2, 128>(p, part, b0, b1, s);
-        case 3: return launch_noflag_t<4, 2, 3, 128>(p, part, b0, b1, s);
-        case 4: return launch_noflag_t<4, 2, 4, 128>(p, part, b0, b1, s);
-        default: return launch_noflag_t<2, 2, 8, 128>(p, part, b0, b1, s);
+        case 1: return launch_noflag_t<4, 2, 1, 128>(p, part, b0, b1, rt, s);
+        case 2: return launch_noflag_t<4, 2, 2, 128>(p, part, b0, b1, rt, s);
+        case 3: return launch_noflag_t<4, 2, 3, 128>(p, part, b0, b1, rt, s);
+        case 4: return launch_noflag_t<4, 2, 4, 128>(p, part, b0, b1, rt, s);
+        default: return launch_noflag_t<2, 2, 8, 128>(p, part, b0, b1, rt, s);
     }
 }
 
-cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s) {
+cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s, RowTiles rt) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_flag_t<2, 1, 128>(p, part, s);
-        case 2: return launch_flag_t<2, 2, 128>(p, part, s);
-        case 3: return launch_flag_t<2, 3, 128>(p, part, s);
-        case 4: return launch_flag_t<2, 4, 128>(p, part, s);
-        default: return launch_flag_t<2, 8, 128>(p, part, s);
+        case 1: return launch_flag_t<2, 1, 128>(p, part, rt, s);
+        case 2: return launch_flag_t<2, 2, 128>(p, part, rt, s);
+        case 3: return launch_flag_t<2, 3, 128>(p, part, rt, s);
+        case 4: return launch_flag_t<2, 4, 128>(p, part, rt, s);
+        default: return launch_flag_t<2, 8, 128>(p, part, rt, s);
     }
 }
 

@@ -21,12 +21,27 @@ TileShape flag_shape(const Problem &p);
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// A range of row tiles [begin, end).  Every kernel family tiles G' rows in
+// pairs (RG = 2), so a row-pair range means the same rows to all of them;
+// the default covers every row.  Launches over parts of the rows write the
+// same partial slots as one launch over all of them.
+struct RowTiles {
+    int begin = 0, end = -1;  // end < 0: to the last row tile
+    RowTiles clip(int row_tiles) const {
+        RowTiles r;
+        r.begin = begin < 0 ? 0 : (begin > row_tiles ? row_tiles : begin);
+        r.end = (end < 0 || end > row_tiles) ? row_tiles : end;
+        return r;
+    }
+};
+
 // Unoccupied bands [band_begin, band_end), FP64.  Writes one ach partial per
 // (row tile, band tile) block and, when part.n1 is set, per-band partials.
 cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int band_begin,
-                               int band_end, cudaStream_t s);
+                               int band_end, cudaStream_t s, RowTiles rows = RowTiles());
 // Occupied bands [0, nvband): full ssxt_scht_solver branch logic in FP64.
-cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s);
+cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s,
+                             RowTiles rows = RowTiles());
 // Static term (reduce_achstemp) over all bands: one partial per block.
 int achstemp_blocks(const Problem &p);
 cudaError_t launch_achstemp(const Problem &p, double2 *partials, int *err, cudaStream_t s);
@@ -51,9 +66,10 @@ TileShape mixed_noflag_shape(const Problem &p);
 // [band_begin, band_end) for the unoccupied kernel, [0, nvband) for the
 // occupied one.
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws,
-                                int band_begin, int band_end, cudaStream_t s, int variant);
+                                int band_begin, int band_end, cudaStream_t s, int variant,
+                                RowTiles rows = RowTiles());
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
-                              cudaStream_t s);
+                              cudaStream_t s, RowTiles rows = RowTiles());
 // Pipeline variants of the mixed kernel, selectable per call (autotuner).
 int mixed_variant_count();
 const char *mixed_variant_name(int variant);
@@ -64,6 +80,12 @@ struct SplitPlanes;
 SplitPlanes split_planes_at(const Problem &p, void *split_ws);
 cudaError_t launch_split(const Problem &p, void *split_ws, int band_begin, int band_end,
                          cudaStream_t s);
+// The same in two steps: the bands (and the reset of the row masks), then
+// the rows of a range of row pairs; every row pair must be split before the
+// tiles that read it.
+cudaError_t launch_split_bands(const Problem &p, void *split_ws, int band_begin, int band_end,
+                               cudaStream_t s);
+cudaError_t launch_split_rows(const Problem &p, void *split_ws, RowTiles pairs, cudaStream_t s);
 
 // Persistent batched launches (gpp_batched.cu): a work queue of tiles over
 // many states.  kind 0 = occupied-band tile (band_tile is the band), 1 =

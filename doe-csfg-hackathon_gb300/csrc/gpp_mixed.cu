@@ -53,12 +53,13 @@ size_t mask_words(const Problem &p) {
 // The same pass sets the row pairs' value-bucket masks: lanes that share a
 // mask word OR their bits together and one of them updates the word (the
 // result does not depend on the order).
-__global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s) {
+__global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s, int pair0,
+                                                         int pair1) {
     const size_t nc = (size_t)p.nc;
-    const size_t n = (size_t)((p.ng + 1) / 2) * nc;
+    const size_t n = (size_t)(pair1 - pair0) * nc;
     const size_t nmw = (nc + kMaskCols - 1) / kMaskCols;
     for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
-        const size_t j = i / nc, ig = i - j * nc;
+        const size_t j = pair0 + i / nc, ig = i % nc;
         const size_t r0 = 2 * j, r1 = min(2 * j + 1, (size_t)p.ng - 1);
         const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
         const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
@@ -101,14 +102,15 @@ __global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes
 template <int RNW, int RG, int NWC, int NWARP, int KC, int NSTAGE, int SYNC, int GROUP, int MINB>
 __global__ void __launch_bounds__(NWARP * 32, MINB)
 mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int band_end,
-                    int row_tiles, int band_tiles) {
-    // Grouped tile order: GROUP consecutive row tiles share each band tile,
-    // so a group's row planes stay in L2 while the band tiles stream past.
+                    int row_tile0, int rows_here, int row_tiles, int band_tiles) {
+    // Grouped tile order over this launch's row tiles [row_tile0, +rows_here):
+    // GROUP consecutive row tiles share each band tile, so a group's row
+    // planes stay in L2 while the band tiles stream past.
     const int tiles_per_group = GROUP * band_tiles;
     const int grp = blockIdx.x / tiles_per_group;
     const int in_grp = blockIdx.x - grp * tiles_per_group;
-    const int rows_in_grp = min(GROUP, row_tiles - grp * GROUP);
-    const int row_tile = grp * GROUP + in_grp % rows_in_grp;
+    const int rows_in_grp = min(GROUP, rows_here - grp * GROUP);
+    const int row_tile = row_tile0 + grp * GROUP + in_grp % rows_in_grp;
     const int band_tile = in_grp / rows_in_grp;
     mixed_tile<RNW, RG, NWC, NWARP, KC, NSTAGE, SYNC>(
         p, part, s, band_begin, band_end, row_tile, band_tile, blockIdx.y,
@@ -137,9 +139,11 @@ constexpr int kNumMixedVariants = sizeof(kMixedVariants) / sizeof(kMixedVariants
 
 template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC, int MINB = 0>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
-                           int b1, cudaStream_t st) {
+                           int b1, RowTiles rt, cudaStream_t st) {
     constexpr int BN = kWarps * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
+    const RowTiles r = rt.clip(row_tiles);
+    if (r.end <= r.begin) return cudaSuccess;
     const size_t smem = sizeof(float4) * NSTAGE * (2 * RG + BN) * KC;
     // The 8-frequency tile holds 64 accumulator registers: keep it at three
     // resident blocks unless the variant asks for more.
@@ -150,21 +154,25 @@ cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPl
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)row_tiles * band_tiles, ceil_div(p.nw, NWC));
-    kern<<<grid, kWarps * 32, smem, st>>>(p, part, s, b0, b1, row_tiles, band_tiles);
+    dim3 grid((unsigned)(r.end - r.begin) * band_tiles, ceil_div(p.nw, NWC));
+    kern<<<grid, kWarps * 32, smem, st>>>(p, part, s, b0, b1, r.begin, r.end - r.begin, row_tiles,
+                                          band_tiles);
     count_launch();
     return cudaGetLastError();
 }
 
 template <int RNW, int RG, int NWC>
 cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
-                                 const SplitPlanes &s, int b0, int b1, cudaStream_t st) {
+                                 const SplitPlanes &s, int b0, int b1, RowTiles rt,
+                                 cudaStream_t st) {
     switch (v) {
-        case 0: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, st);
-        case 2: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, st);
-        case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, st);
-        case 4: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, st);
-        default: return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
+        case 0: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 2: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, rt, st);
+        case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, rt, st);
+        case 4:
+            return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, rt, st);
+        default:
+            return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
     }
 }
 
@@ -194,66 +202,87 @@ size_t mixed_split_bytes(const Problem &p) {
 
 SplitPlanes split_planes_at(const Problem &p, void *split_ws) { return planes(p, split_ws); }
 
-cudaError_t launch_split(const Problem &p, void *split_ws, int b0, int b1, cudaStream_t st) {
-    const SplitPlanes s = planes(p, split_ws);
+static int split_blocks() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = sms > 0 ? sms * 8 : 1024;
+    return sms > 0 ? sms * 8 : 1024;
+}
+
+cudaError_t launch_split_bands(const Problem &p, void *split_ws, int b0, int b1, cudaStream_t st) {
+    const SplitPlanes s = planes(p, split_ws);
     cudaError_t e = cudaMemsetAsync(s.masks, 0, sizeof(unsigned long long) * mask_words(p), st);
     if (e != cudaSuccess) return e;
-    split_rows_kernel<<<blocks, 256, 0, st>>>(p, s);
-    split_bands_kernel<<<blocks, 256, 0, st>>>(p, s, b0, b1);
-    count_launch(2);
+    split_bands_kernel<<<split_blocks(), 256, 0, st>>>(p, s, b0, b1);
+    count_launch();
     return cudaGetLastError();
+}
+
+cudaError_t launch_split_rows(const Problem &p, void *split_ws, RowTiles pairs, cudaStream_t st) {
+    const RowTiles r = pairs.clip((p.ng + 1) / 2);
+    if (r.end <= r.begin) return cudaSuccess;
+    split_rows_kernel<<<split_blocks(), 256, 0, st>>>(p, planes(p, split_ws), r.begin, r.end);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split(const Problem &p, void *split_ws, int b0, int b1, cudaStream_t st) {
+    cudaError_t e = launch_split_bands(p, split_ws, b0, b1, st);
+    if (e == cudaSuccess) e = launch_split_rows(p, split_ws, RowTiles(), st);
+    return e;
 }
 
 template <int RG, int NWC, int THREADS, int SEM>
 __global__ void __launch_bounds__(THREADS)
-flag_mixed_kernel(Problem p, Partials part, SplitPlanes s) {
+flag_mixed_kernel(Problem p, Partials part, SplitPlanes s, int row_tile0, int row_tiles) {
     constexpr int K = RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, blockIdx.x, blockIdx.y, blockIdx.z,
-                                           (long long)blockIdx.y * gridDim.x + blockIdx.x, red, S);
+    const int row_tile = row_tile0 + blockIdx.x;
+    flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, row_tile, blockIdx.y, blockIdx.z,
+                                           (long long)blockIdx.y * row_tiles + row_tile, red, S);
 }
 
 template <int NWC>
 cudaError_t launch_flag_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s,
-                                cudaStream_t st) {
-    dim3 grid(ceil_div(p.ng, 2), p.nv, ceil_div(p.nw, NWC));
+                                RowTiles rt, cudaStream_t st) {
+    const int row_tiles = ceil_div(p.ng, 2);
+    const RowTiles r = rt.clip(row_tiles);
+    if (r.end <= r.begin) return cudaSuccess;
+    dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
     if (p.semantics == kSemKerSeq)
-        flag_mixed_kernel<2, NWC, 128, kSemKerSeq><<<grid, 128, 0, st>>>(p, part, s);
+        flag_mixed_kernel<2, NWC, 128, kSemKerSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
+                                                                        row_tiles);
     else
-        flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(p, part, s);
+        flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
+                                                                            row_tiles);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
-                              cudaStream_t st) {
+                              cudaStream_t st, RowTiles rt) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
     const SplitPlanes s = planes(p, split_ws);
     switch (nwc_for(p.nw)) {
-        case 1: return launch_flag_mixed_t<1>(p, part, s, st);
-        case 2: return launch_flag_mixed_t<2>(p, part, s, st);
-        case 3: return launch_flag_mixed_t<3>(p, part, s, st);
-        case 4: return launch_flag_mixed_t<4>(p, part, s, st);
-        default: return launch_flag_mixed_t<8>(p, part, s, st);
+        case 1: return launch_flag_mixed_t<1>(p, part, s, rt, st);
+        case 2: return launch_flag_mixed_t<2>(p, part, s, rt, st);
+        case 3: return launch_flag_mixed_t<3>(p, part, s, rt, st);
+        case 4: return launch_flag_mixed_t<4>(p, part, s, rt, st);
+        default: return launch_flag_mixed_t<8>(p, part, s, rt, st);
     }
 }
 
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws, int b0,
-                                int b1, cudaStream_t st, int variant) {
+                                int b1, cudaStream_t st, int variant, RowTiles rt) {
     if (b1 <= b0 || p.ng == 0) return cudaSuccess;
     const SplitPlanes s = planes(p, split_ws);
-    cudaError_t e = cudaSuccess;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_mixed_t<1, 2, 1, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
-        case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
-        case 3: return launch_mixed_variant<1, 2, 3>(variant, p, part, s, b0, b1, st);
-        case 4: return launch_mixed_t<1, 2, 4, 128, 3, kSyncBlock>(p, part, s, b0, b1, st);
-        default: return launch_mixed_variant<1, 2, 8>(variant, p, part, s, b0, b1, st);
+        case 1: return launch_mixed_t<1, 2, 1, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 3: return launch_mixed_variant<1, 2, 3>(variant, p, part, s, b0, b1, rt, st);
+        case 4: return launch_mixed_t<1, 2, 4, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        default: return launch_mixed_variant<1, 2, 8>(variant, p, part, s, b0, b1, rt, st);
     }
 }
 

@@ -142,19 +142,23 @@ def test_device_side_index_fault_is_reported_then_cleared():
         o.wait()
 
 
-def test_host_path_equals_device_path():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("ngpown", [20, 3, 33])
+def test_host_path_equals_device_path(precision, ngpown):
+    """The host path copies the G' rows in pieces and starts each piece's
+    kernels when its rows land; the bits must equal one device-path call."""
     o = ops()
-    inp = W.make_inputs(W.Shape(12, 3, 1000, 20, 3), 51)
+    inp = W.make_inputs(W.Shape(12, 3, 1000, ngpown, 3, near_pole=0.05), 51)
     d = o.DeviceInputs.from_host(inp)
-    dev = o.sigma(d, "fp64", acht_n1=True, achstemp=True)
+    dev = o.sigma(d, precision, acht_n1=True, achstemp=True)
     o.wait()
     arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
                                            "vcoul", "inv_igp_index", "indinv", "wx_array")}
     with o.HostContext() as ctx:
         with pytest.raises(capi.GppError):
             ctx.last_timing()  # nothing timed yet
-        host = ctx.sigma(arrays, inp.shape, "fp64", acht_n1=True, achstemp=True)
-        host2 = ctx.sigma(arrays, inp.shape, "fp64", acht_n1=True, achstemp=True)
+        host = ctx.sigma(arrays, inp.shape, precision, acht_n1=True, achstemp=True)
+        host2 = ctx.sigma(arrays, inp.shape, precision, acht_n1=True, achstemp=True)
         t = ctx.last_timing()
     assert t["h2d_ms"] > 0 and t["compute_ms"] > 0 and t["d2h_ms"] >= 0
     for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
