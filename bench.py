@@ -46,6 +46,16 @@ FLOPS_PER_TERM_BASE = 20.0
 FLOPS_PER_TRIPLE = 12.0
 
 
+def mixed_fp32_ops_per_term(nwc: int) -> float:
+    """FP32 operations the mixed kernel issues per unoccupied term, counted
+    from its column routine: per ig column a thread issues 44 packed
+    instructions shared by its frequencies (A = aqsn*Q, A*Im(wtilde),
+    Im(wtilde)^2) and 75 per frequency (wdiff, |wdiff|^2, reciprocal, the two
+    products, the two accumulations), each packed instruction doing one FP32
+    operation for each of the tile's two rows."""
+    return (44.0 + 75.0 * nwc) / nwc
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) of SM clock and throttle reasons."""
 
@@ -397,8 +407,19 @@ def main() -> int:
     kname = "mixed_noflag_kernel" if precision == "mixed" else "noflag_fp64_kernel"
     traffic = profile_traffic(kname, args.workload, precision)
     pipe_file = "ncu_noflag_mixed_profile.txt" if precision == "mixed" else "ncu_noflag_fp64_profile.txt"
-    pipe_metric = "sm__inst_executed_pipe_fma" if precision == "mixed" else "sm__inst_executed_pipe_fp64"
+    # Pipe busy cycles: a packed f32x2 instruction occupies the FMA pipe for
+    # two cycles, so instruction counts understate its load.
+    pipe_metric = "sm__pipe_fma_cycles_active" if precision == "mixed" else "sm__inst_executed_pipe_fp64"
     pipe_pct = profile_pipe(pipe_file, pipe_metric)
+    issued = None
+    if precision == "mixed" and kms and fp32_peak:
+        ops = mixed_fp32_ops_per_term(shape.nw if shape.nw <= 4 else 8)
+        rate = ops * unocc_terms / (kms * 1e-3)  # FP32 operations per second
+        issued = {"fp32_ops_per_term": ops, "achieved_tops": rate * 1e-12,
+                  "peak_tops": fp32_peak / 2.0, "frac": rate / (fp32_peak / 2.0 * 1e12),
+                  "note": "issued FP32 operations (float-float emulation included) against the "
+                          "measured FP32 FMA rate; 'frac' above counts algorithmic FP64-equivalent "
+                          "flops only"}
     roofline = {"bound": "fp32" if precision == "mixed" else "fp64",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if (achieved and peak) else None,
@@ -412,6 +433,8 @@ def main() -> int:
                 "traffic_note": "dram read+write bytes per launch at this workload, "
                                 f"profiles/launches_{args.workload}_{precision}.txt",
                 "fp64_fma_peak_tflops": fp64_peak, "fp32_fma_peak_tflops": fp32_peak}
+    if issued:
+        roofline["issued"] = issued
 
     line = {"metric": METRIC, "value": ws * nterms / (ms * 1e-3), "unit": "terms/s",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,

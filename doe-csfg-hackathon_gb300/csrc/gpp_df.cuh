@@ -78,8 +78,10 @@ __host__ __device__ __forceinline__ df df_norm(df a) {
     return {s, fsub(a.l, fsub(s, a.h))};
 }
 // 1/d for a normalised d: hardware reciprocal seed r of d.h (MUFU, relative
-// error ~2^-23) and one Newton-Raphson correction r e, e = 1 - d r computed
-// against the full df value of d; error ~2^-45.
+// error ~2^-23) and a second-order Newton-Raphson correction r (e + e^2),
+// e = 1 - d r computed against the full df value; error ~2^-45 and, unlike
+// the first-order step (always short by r e^2), without a sign preference
+// that long sums would accumulate.
 __host__ __device__ __forceinline__ df df_rcp(df d) {
     float r;
 #ifdef __CUDA_ARCH__
@@ -89,6 +91,7 @@ __host__ __device__ __forceinline__ df df_rcp(df d) {
 #endif
     float e = fmaf(-d.h, r, 1.0f);
     e = fmaf(-d.l, r, e);
+    e = fmaf(e, e, e);
     return {r, fmul(r, e)};
 }
 __host__ __device__ __forceinline__ df split(double x) {

@@ -101,31 +101,38 @@ __host__ __device__ __forceinline__ df2 df2_mul(const df2 &a, const df2 &b) {
     e = f2fma(a.l, b.h, e);
     return {p, e};
 }
-// (h + l)^2 including l*l, so the square stays accurate when l is a sizeable
-// fraction of h (an unnormalised difference after cancellation).
-__host__ __device__ __forceinline__ df2 df2_sqr_full(const df2 &a) {
+// (h + l)^2 for a normalised value (the l*l term, below 2^-48 of the
+// result, is left out).
+__host__ __device__ __forceinline__ df2 df2_sqr(const df2 &a) {
     const float2 p = f2mul(a.h, a.h);
     float2 e = f2fma(a.h, a.h, f2neg(p));
     e = f2fma(f2add(a.h, a.h), a.l, e);
-    e = f2fma(a.l, a.l, e);
     return {p, e};
 }
-// 1/d per lane: hardware reciprocal seed (MUFU, relative error ~2^-23) and
-// one Newton-Raphson correction against the full df value.  The seed is
-// taken of fl(d.h + d.l), not of d.h: d may be unnormalised (|d.l| up to
-// ~1e-4 |d.h| after a cancelling wdiff), and one Newton step leaves the
-// square of the seed's relative error.
+// Renormalise both lanes so that |l| <= ulp(h)/2 (Fast2Sum, Dekker 1971),
+// after a cancelling subtraction.  Products of an unnormalised operand drop
+// an l*l term that is then no longer negligible, and on sums of ~1e10 terms
+// that small, one-signed error shows up at the 1e-10 level.
+__host__ __device__ __forceinline__ df2 df2_norm(const df2 &a) {
+    const float2 s = f2add(a.h, a.l);
+    return {s, f2sub(a.l, f2sub(s, a.h))};
+}
+// 1/d per lane: hardware reciprocal seed r of d.h (MUFU, relative error
+// below ~2^-23) and a second-order Newton-Raphson correction,
+// r (1 + e + e^2) with e = 1 - d r computed against the full df value.  The
+// first-order step alone leaves a one-signed error of -e^2, which long sums
+// would accumulate.
 __host__ __device__ __forceinline__ df2 df2_rcp(const df2 &d) {
-    const float2 s = f2add(d.h, d.l);
     float2 r;
 #ifdef __CUDA_ARCH__
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.x) : "f"(s.x));
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.y) : "f"(s.y));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.x) : "f"(d.h.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.y) : "f"(d.h.y));
 #else
-    r = make_float2(1.0f / s.x, 1.0f / s.y);
+    r = make_float2(1.0f / d.h.x, 1.0f / d.h.y);
 #endif
     float2 e = f2fma(f2neg(d.h), r, f2(1.0f, 1.0f));
     e = f2fma(f2neg(d.l), r, e);
+    e = f2fma(e, e, e);
     return {r, f2mul(r, e)};
 }
 

@@ -11,7 +11,7 @@
 // errors of the main path are captured exactly; only second-order cross
 // terms round in FP32, so each term carries ~2^-44 relative error, far below
 // the 1e-8 target.  A block's two G' rows are the two lanes of the packed
-// f32x2 instructions (gpp_df2.cuh), so a term costs ~44 packed FP32
+// f32x2 instructions (gpp_df2.cuh), so a term costs ~45 packed FP32
 // instructions instead of ~11 FP64 ones (~700 FP32-equivalents).
 //
 // FP64 is kept where stability needs it:
@@ -134,6 +134,7 @@ constexpr MixedVariant kMixedVariants[] = {
     {128, 2, kSyncRing, 0, "mbarrier ring, 2 x 128 columns"},
     {64, 4, kSyncRing, 0, "mbarrier ring, 4 x 64 columns"},
     {128, 2, kSyncBlock, 5, "block-sync, 2 x 128 columns, 5 blocks/SM"},
+    {128, 3, kSyncRing, 0, "mbarrier ring, 3 x 128 columns"},
 };
 constexpr int kNumMixedVariants = sizeof(kMixedVariants) / sizeof(kMixedVariants[0]);
 
@@ -171,6 +172,7 @@ cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
         case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, rt, st);
         case 4:
             return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, rt, st);
+        case 5: return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncRing>(p, part, s, b0, b1, rt, st);
         default:
             return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
     }

@@ -157,9 +157,11 @@ static __device__ __noinline__ TermPair pole_pair(const Problem &p, df2 d, float
 // acc.  Every value is a df2 whose lanes are rows row0 and row0 + 1, so one
 // packed f32x2 instruction advances both rows' terms; the row-pair planes
 // load straight into lane pairs and band values broadcast to both lanes.
-// Re(wdiff) is left unnormalised after its cancelling subtraction; its
-// square keeps the l*l term and the reciprocal is seeded from h + l, which
-// keeps the per-term error near 2^-44 relative.  With CHECK, terms within
+// Re(wdiff) is renormalised after its cancelling subtraction and the
+// reciprocal carries a second-order correction: both keep the per-term error
+// near 2^-44 relative and free of a sign preference (an unnormalised wdiff
+// or a first-order reciprocal biases every term the same way, and sums of
+// 1e10 terms turn a 1e-15 bias into 1e-10).  With CHECK, terms within
 // 1e-3 |wx| of the pole are recomputed in FP64 from the inputs; tiles call
 // the CHECK = false form only when no wtilde can come that near any of the
 // warp's wx values.
@@ -187,8 +189,8 @@ __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
         const df2 Ar_wti = df2_mul(Ar, wti);
 #pragma unroll
         for (int w = 0; w < NWC; ++w) {
-            const df2 wr = df2_sub(df2_bcast(wx[n][w]), wtr);  // Re(wdiff)
-            const df2 d = df2_add(df2_sqr_full(wr), wti2);    // |wdiff|^2
+            const df2 wr = df2_norm(df2_sub(df2_bcast(wx[n][w]), wtr));  // Re(wdiff)
+            const df2 d = df2_add(df2_sqr(wr), wti2);                     // |wdiff|^2
             const df2 r = df2_rcp(d);
             // A conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
             df2 tre = df2_mul(df2_sub(df2_mul(Ar, wr), Ai_wti), r);
