@@ -125,3 +125,20 @@ def test_terms_at_the_pole_take_the_fp64_path(semantics):
     o.wait()
     assert rel_err(b.achtemp.cpu().numpy(), a.achtemp.cpu().numpy()) <= MIXED_TOL
     assert rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy()) <= MIXED_TOL
+
+
+def test_long_sums_carry_no_per_term_bias():
+    """32 frequencies, 8 occupied bands, ~1.7e9 terms per frequency, no
+    near-pole wtilde: a per-term error of one sign (a first-order reciprocal,
+    an unnormalised wdiff) grows with the square root of the term count and
+    showed up here at ~1e-10; unbiased float-float terms stay far below."""
+    o = ops()
+    shape = W.Shape(64, 8, 65536, 400, 32, dw=0.25)
+    d = o.device_inputs(shape, 20240607)
+    a = o.sigma(d, "fp64")
+    b = o.sigma(d, "mixed")
+    o.wait()
+    ea = rel_err(b.achtemp.cpu().numpy(), a.achtemp.cpu().numpy())
+    ex = rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy())
+    print(f"mixed vs fp64: achtemp {ea:.3e}, asxtemp {ex:.3e}")
+    assert ea <= 5e-11 and ex <= 5e-11
