@@ -16,6 +16,9 @@
  *   oracle_sigma      driver loop nest   gppComplex_seq.cpp:335-383
  *   oracle_sigma_omp  OpenMP loop shape  gppOpenMP3.cpp:278-333
  *   oracle_ramp_inputs ramp init         gppKerSeq.cpp:225-258
+ *   oracle_sigma_extended  the same sums in long double with compensated
+ *                          accumulation: a reference value for measuring the
+ *                          FP64 paths' own rounding (no operation-order parity)
  */
 #include "gpp_oracle.h"
 
@@ -321,4 +324,158 @@ void oracle_ramp_inputs(int nb, int nc, int ng, int nw,
         wx[iw] = e_lk - e_n1kq + dw * ((iw + 1) - 2);
         if (fabs(wx[iw]) < GPP_TO1) wx[iw] = GPP_TO1;
     }
+}
+
+/* ------------------------------------------------------------------------
+ * Extended-precision reference: the algebra of the functions above (same
+ * branches, cutoff and semantics), evaluated in long double -- 64-bit
+ * significand on x86-64, 113-bit on aarch64 -- with Neumaier-compensated
+ * sums over ig and over the (n1, my_igp) pairs.  It does not follow the
+ * reference's operation order; it serves as the "true" value against which
+ * both the FP64 oracle and the GPU paths show their rounding error.  Branch
+ * decisions can differ from FP64 only for terms within rounding distance of
+ * a threshold.
+ */
+typedef long double ld;
+typedef struct { ld re, im; } cxl;
+typedef struct { ld s, c; } ksum; /* Neumaier running sum: s + c */
+
+static inline cxl mkl(ld re, ld im) { cxl z; z.re = re; z.im = im; return z; }
+static inline cxl cxl_of(cx a) { return mkl(a.re, a.im); }
+static inline cxl mull(cxl a, cxl b) { return mkl(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+static inline cxl conjl_(cxl a) { return mkl(a.re, -a.im); }
+static inline cxl scalel(cxl a, ld s) { return mkl(a.re * s, a.im * s); }
+static inline ld norm2l(cxl a) { return a.re * a.re + a.im * a.im; }
+static inline void kadd(ksum *k, ld x)
+{
+    const ld t = k->s + x;
+    if (fabsl(k->s) >= fabsl(x)) k->c += (k->s - t) + x;
+    else k->c += (x - t) + k->s;
+    k->s = t;
+}
+static inline ld kval(const ksum *k) { return k->s + k->c; }
+
+static void term_l(int sem, ld wxt, cxl wt, cxl ieps, cxl *ssx_out, cxl *sch_out)
+{
+    cxl sch = mkl(0, 0), ssx = mkl(0, 0);
+    const cxl wt2 = mull(wt, wt), omega2 = mull(wt2, ieps);
+    const cxl wdiff = mkl(wxt - wt.re, -wt.im);
+    const ld rden = 1.0L / norm2l(wdiff);
+    const cxl delw = scalel(mull(wt, conjl_(wdiff)), rden);
+    const ld delwr = norm2l(delw), wdiffr = norm2l(wdiff);
+    if (wdiffr > (ld)GPP_LIMITTWO && delwr < (ld)GPP_LIMITONE) {
+        sch = mull(delw, ieps);
+        ssx = scalel(omega2, 1.0L / (wxt * wxt));
+    } else if (delwr > (ld)GPP_TO1) {
+        const cxl cden = scalel(mull(wt2, mkl(0.5L + delw.re, delw.im)), 4.0L);
+        const cxl t = mull(mkl(-omega2.re, -omega2.im), conjl_(cden));
+        ssx = mull(t, scalel(delw, 1.0L / norm2l(cden)));
+    }
+    if (sem == ORACLE_SEM_COMPLEX_SEQ && wxt < 0 && sqrtl(norm2l(ssx)) > sqrtl(norm2l(ieps)) * 4.0L)
+        ssx = mkl(0, 0);
+    *ssx_out = ssx;
+    *sch_out = sch;
+}
+
+/* Per (n1, my_igp, iw): compensated sums of the ig terms. */
+static void pair_l(const oracle_problem *p, int n1, int my_igp, int iw, cxl *sch, cxl *ssx)
+{
+    const int nc = p->ncouls;
+    const cx *wrow = p->wtilde_array + (size_t)my_igp * nc;
+    const cx *erow = p->I_eps_array + (size_t)my_igp * nc;
+    const cx *nrow = p->aqsntemp + (size_t)n1 * nc;
+    const int igp = clamp_igp(p, my_igp);
+    const cxl m = conjl_(cxl_of(p->aqsmtemp[(size_t)n1 * nc + igp]));
+    const ld wxt = p->wx_array[(size_t)n1 * p->wx_stride + iw];
+    ksum hr = {0, 0}, hi = {0, 0}, xr = {0, 0}, xi = {0, 0};
+    for (int ig = 0; ig < nc; ++ig) {
+        const cxl wt = cxl_of(wrow[ig]), ie = cxl_of(erow[ig]);
+        const cxl matng = mull(cxl_of(nrow[ig]), m);
+        if (n1 < p->nvband) {
+            cxl x, h;
+            term_l(p->semantics, wxt, wt, ie, &x, &h);
+            const cxl a = mull(matng, h), b = mull(matng, x);
+            kadd(&hr, a.re); kadd(&hi, a.im); kadd(&xr, b.re); kadd(&xi, b.im);
+        } else {
+            const cxl wdiff = mkl(wxt - wt.re, -wt.im);
+            const cxl delw = scalel(mull(wt, conjl_(wdiff)), 1.0L / norm2l(wdiff));
+            const cxl a = mull(matng, mull(delw, ie));
+            kadd(&hr, a.re); kadd(&hi, a.im);
+        }
+    }
+    *sch = mkl(kval(&hr), kval(&hi));
+    *ssx = mkl(kval(&xr), kval(&xi));
+}
+
+int oracle_sigma_extended(const oracle_problem *p, oracle_outputs *o, int nthreads)
+{
+    if (validate(p, o)) return -1;
+    zero_outputs(p, o);
+    const int nw = p->nw, ng = p->ngpown;
+    const int nbands = p->band_end - p->band_begin;
+    if (nbands == 0 || ng == 0) return 0;
+    const size_t npairs = (size_t)nbands * (size_t)ng;
+    /* Per pair and frequency: ach re/im, asx re/im; per pair: static term. */
+    ld *v = (ld *)malloc(sizeof(ld) * npairs * ((size_t)nw * 4 + 2));
+    if (!v) return -2;
+    if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+    for (long long pr = 0; pr < (long long)npairs; ++pr) {
+        const int n1 = p->band_begin + (int)(pr / ng);
+        const int my_igp = (int)(pr % ng);
+        const int igp = clamp_igp(p, my_igp);
+        const ld vc = p->vcoul[igp];
+        ld *row = v + (size_t)pr * ((size_t)nw * 4 + 2);
+        for (int iw = 0; iw < nw; ++iw) {
+            cxl sch, ssx;
+            pair_l(p, n1, my_igp, iw, &sch, &ssx);
+            row[4 * iw + 0] = sch.re * 0.5L * vc;
+            row[4 * iw + 1] = sch.im * 0.5L * vc;
+            row[4 * iw + 2] = ssx.re * (ld)p->occ * vc;
+            row[4 * iw + 3] = ssx.im * (ld)p->occ * vc;
+        }
+        /* static term (achstemp_row) */
+        const int nc = p->ncouls;
+        const cxl m = conjl_(cxl_of(p->aqsmtemp[(size_t)n1 * nc + igp]));
+        const cxl ie = cxl_of(p->I_eps_array[(size_t)my_igp * nc + igp]);
+        const cxl schs = mkl(-ie.re, -ie.im);
+        cxl st = mkl(0, 0);
+        if (sqrtl(norm2l(schs)) > (ld)GPP_TO1)
+            st = scalel(mull(mull(cxl_of(p->aqsntemp[(size_t)n1 * nc + igp]), m), schs), vc * 0.5L);
+        row[4 * nw] = st.re;
+        row[4 * nw + 1] = st.im;
+    }
+    for (int iw = 0; iw < nw; ++iw) {
+        ksum ar = {0, 0}, ai = {0, 0}, xr = {0, 0}, xi = {0, 0};
+        for (size_t pr = 0; pr < npairs; ++pr) {
+            const ld *row = v + pr * ((size_t)nw * 4 + 2);
+            kadd(&ar, row[4 * iw]); kadd(&ai, row[4 * iw + 1]);
+            if (p->band_begin + (int)(pr / ng) < p->nvband) {
+                kadd(&xr, row[4 * iw + 2]); kadd(&xi, row[4 * iw + 3]);
+            }
+        }
+        o->achtemp[iw] = mk((double)kval(&ar), (double)kval(&ai));
+        o->asxtemp[iw] = mk((double)kval(&xr), (double)kval(&xi));
+    }
+    if (o->acht_n1_loc && nw >= 3)
+        for (int n1 = p->band_begin; n1 < p->band_end; ++n1) {
+            ksum ar = {0, 0}, ai = {0, 0};
+            for (int g = 0; g < ng; ++g) {
+                const ld *row = v + ((size_t)(n1 - p->band_begin) * ng + g) * ((size_t)nw * 4 + 2);
+                kadd(&ar, row[8]); kadd(&ai, row[9]);
+            }
+            o->acht_n1_loc[n1] = mk((double)kval(&ar), (double)kval(&ai));
+        }
+    if (o->achstemp) {
+        ksum ar = {0, 0}, ai = {0, 0};
+        for (size_t pr = 0; pr < npairs; ++pr) {
+            const ld *row = v + pr * ((size_t)nw * 4 + 2);
+            kadd(&ar, row[4 * nw]); kadd(&ai, row[4 * nw + 1]);
+        }
+        o->achstemp[0] = mk((double)kval(&ar), (double)kval(&ai));
+    }
+    free(v);
+    return 0;
 }

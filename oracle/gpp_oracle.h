@@ -75,6 +75,14 @@ void oracle_ramp_inputs(int number_bands, int ncouls, int ngpown, int nw,
                         oracle_complex *I_eps_array, oracle_complex *wtilde_array,
                         double *vcoul, int *inv_igp_index, double *wx_array);
 
+/* The same sums evaluated in long double (64-bit significand on x86-64,
+ * 113-bit on aarch64) with Neumaier-compensated accumulation: a reference
+ * value to measure the rounding error of the FP64 and GPU paths against.
+ * It follows the reference's algebra and branches but not its operation
+ * order, so it is not bit-comparable with the reference.  Same return codes
+ * as oracle_sigma. */
+int oracle_sigma_extended(const oracle_problem *p, oracle_outputs *out, int nthreads);
+
 int oracle_max_threads(void);
 
 #ifdef __cplusplus

@@ -42,7 +42,7 @@ def _load(kind: str) -> C.CDLL:
         return _libs[kind]
     if kind == "oracle":
         lib = C.CDLL(build_oracle.build_oracle())
-        for fn in (lib.oracle_sigma, lib.oracle_sigma_omp):
+        for fn in (lib.oracle_sigma, lib.oracle_sigma_omp, lib.oracle_sigma_extended):
             fn.restype = C.c_int
             fn.argtypes = [C.POINTER(_Problem), C.POINTER(_Outputs), C.c_int]
         lib.oracle_max_threads.restype = C.c_int
@@ -72,6 +72,8 @@ def run(inp, semantics: str = "complex_seq", nthreads: int = 1, impl: str = "ora
 
     impl: "oracle" (C restatement, sequential order), "oracle_omp" (the
     reference's OpenMP loop shape, order depends on nthreads),
+    "oracle_extended" (long double with compensated sums: a reference value
+    for rounding errors, not bit-comparable with the reference),
     "ref_complex_seq" / "ref_kerseq" (the reference's own functions)."""
     s = inp.shape
     nb = s.number_bands
@@ -97,6 +99,8 @@ def run(inp, semantics: str = "complex_seq", nthreads: int = 1, impl: str = "ora
     o.achstemp = out["achstemp"].ctypes.data
     if impl == "oracle":
         rc = _load("oracle").oracle_sigma(C.byref(p), C.byref(o), nthreads)
+    elif impl == "oracle_extended":
+        rc = _load("oracle").oracle_sigma_extended(C.byref(p), C.byref(o), nthreads)
     elif impl == "oracle_omp":
         o.acht_n1_loc = None
         out["acht_n1_loc"] = None

@@ -142,3 +142,29 @@ def test_long_sums_carry_no_per_term_bias():
     ex = rel_err(b.asxtemp.cpu().numpy(), a.asxtemp.cpu().numpy())
     print(f"mixed vs fp64: achtemp {ea:.3e}, asxtemp {ex:.3e}")
     assert ea <= 5e-11 and ex <= 5e-11
+
+
+@pytest.mark.parametrize("shape", [
+    W.Shape(32, 2, 2048, 64, 3, near_pole=0.01),
+    W.Shape(16, 4, 2048, 33, 32, dw=0.25),
+], ids=["near_pole_3freq", "sweep_32freq"])
+def test_true_error_of_both_paths(shape):
+    """Both GPU paths against the long-double, compensated-sum oracle: the
+    FP64 kernel within FP64 rounding, the mixed kernel far inside its 1e-8
+    budget."""
+    import oracle_py
+    o = ops()
+    inp = W.make_inputs(shape, 41)
+    truth = oracle_py.run(inp, "complex_seq", nthreads=oracle_py.max_threads(),
+                          impl="oracle_extended")
+    d = o.DeviceInputs.from_host(inp)
+    a = o.sigma(d, "fp64")
+    b = o.sigma(d, "mixed")
+    o.wait()
+    errs = {}
+    for name, r in (("fp64", a), ("mixed", b)):
+        errs[name] = max(rel_err(r.achtemp.cpu().numpy(), truth["achtemp"]),
+                         rel_err(r.asxtemp.cpu().numpy(), truth["asxtemp"]))
+    print("error against the extended-precision oracle:", errs)
+    assert errs["fp64"] <= 1e-12
+    assert errs["mixed"] <= 1e-10

@@ -86,3 +86,31 @@ def test_live_reference_agrees_on_fresh_inputs(semantics):
     b = oracle_py.run(inp, semantics, impl="ref_" + semantics)
     for k in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
         np.testing.assert_array_equal(a[k], b[k])
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["kind"] == "seeded"], ids=lambda c: c["name"])
+def test_extended_oracle_agrees_with_reference_outputs(case):
+    """The long-double, compensated-sum oracle is a reference value for the
+    rounding of the FP64 paths: the reference's own FP64 outputs must lie
+    within FP64 summation error of it (per-band sums cancel more, hence the
+    looser bound on acht_n1_loc)."""
+    r = oracle_py.run(case_inputs(case), case["semantics"], nthreads=oracle_py.max_threads(),
+                      impl="oracle_extended")
+    for key, tol in (("achtemp", 1e-12), ("asxtemp", 1e-12), ("achstemp", 1e-12),
+                     ("acht_n1_loc", 1e-10)):
+        want = unhex(case[key])
+        if want is None or r[key] is None:
+            continue
+        g = np.concatenate([r[key].real, r[key].imag])
+        w = np.concatenate([want.real, want.imag])
+        err = np.max(np.abs(g - w) / np.where(w == 0, 1.0, np.abs(w))) if w.size else 0.0
+        assert err <= tol, (key, err)
+
+
+def test_extended_oracle_sees_a_planted_error():
+    inp = W.make_inputs(W.Shape(12, 3, 900, 17, 3), 24)
+    a = oracle_py.run(inp, impl="oracle_extended", nthreads=4)
+    inp.aqsntemp = inp.aqsntemp.copy()
+    inp.aqsntemp[7, 100] *= 1 + 1e-9
+    b = oracle_py.run(inp, impl="oracle_extended", nthreads=4)
+    assert np.max(np.abs(a["achtemp"] - b["achtemp"])) > 0
