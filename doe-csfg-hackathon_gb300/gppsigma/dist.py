@@ -1,10 +1,11 @@
 """Multi-rank bookkeeping for runs with one process per GPU.
 
-GPP sigma states are independent: each rank runs its own state (seed offset
-by rank) and nothing on the data path is exchanged.  Only the timing is
-combined -- the job's time is the slowest rank's -- and, when a caller wants
-one answer for a sharded state, per-rank partial sums are added on rank 0 in
-rank order (fixed order, so the result does not depend on arrival order).
+GPP sigma states are independent: by default each rank runs its own state
+(seed offset by rank) and nothing on the data path is exchanged; only the
+timing is combined -- the job's time is the slowest rank's.  One state can
+also be sharded by G' rows (row_range); then the per-rank partial sums are
+the one exchange step, added on rank 0 in rank order (fixed order, so the
+result does not depend on arrival order).
 """
 from __future__ import annotations
 
@@ -15,6 +16,17 @@ def env() -> tuple[int, int, int]:
     """(world_size, rank, local_rank) from the torchrun environment."""
     return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
             int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def row_range(ngpown: int, rank: int, world: int) -> tuple[int, int]:
+    """G' rows [r0, r1) of one state handled by `rank` when the state is
+    sharded across ranks, as the reference's MPI version splits its my_igp
+    loop (gppMPIOpenMP3.cpp:171-172, partial sums reduced at :360-370).
+    Ranges are contiguous and start on even rows, so each rank's rows form
+    whole row pairs of the mixed-precision tiles."""
+    pairs = (ngpown + 1) // 2
+    p0, p1 = pairs * rank // world, pairs * (rank + 1) // world
+    return min(2 * p0, ngpown), min(2 * p1, ngpown)
 
 
 def state_seed(base: int, rank: int) -> int:

@@ -143,6 +143,13 @@ class DeviceInputs:
     wx_array: "torch.Tensor"
     wx_stride: int
 
+    def rows(self, r0: int, r1: int) -> "DeviceInputs":
+        """The same problem restricted to G' rows [r0, r1) (views, no copy):
+        the row sums of a sharded state, which add up to the full sums."""
+        return dataclasses.replace(self, ngpown=r1 - r0, I_eps_array=self.I_eps_array[r0:r1],
+                                   wtilde_array=self.wtilde_array[r0:r1],
+                                   inv_igp_index=self.inv_igp_index[r0:r1])
+
     @classmethod
     def from_host(cls, inp, device="cuda", with_indinv: bool = True) -> "DeviceInputs":
         s = inp.shape

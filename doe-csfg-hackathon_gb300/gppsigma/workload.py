@@ -127,6 +127,13 @@ class Inputs:
     indinv: np.ndarray        # int32 [nc]
     wx_array: np.ndarray      # float64 [nb][nw]
 
+    def rows(self, r0: int, r1: int) -> "Inputs":
+        """The same problem restricted to G' rows [r0, r1)."""
+        sh = dataclasses.replace(self.shape, ngpown=r1 - r0)
+        return dataclasses.replace(self, shape=sh, I_eps_array=self.I_eps_array[r0:r1],
+                                   wtilde_array=self.wtilde_array[r0:r1],
+                                   inv_igp_index=self.inv_igp_index[r0:r1])
+
     def digest(self) -> str:
         """sha256 over every input array's bytes (generator drift check)."""
         h = hashlib.sha256()

@@ -212,3 +212,19 @@ def test_production_shape_band_partition_and_oracle_subset():
     want = oracle_py.run(sub, "complex_seq", nthreads=max(1, os.cpu_count() or 1))
     assert rel_err(r.achtemp.cpu().numpy(), want["achtemp"]) <= FP64_TOL
     assert rel_err(r.asxtemp.cpu().numpy(), want["asxtemp"]) <= FP64_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_row_shards_add_up_to_the_full_call(precision):
+    """A state sharded by G' rows (one slice per rank in a multi-GPU run):
+    the slices' sums add up to the one-call sums."""
+    from gppsigma import dist as gd
+    o = ops()
+    inp = W.make_inputs(W.Shape(20, 2, 1500, 37, 3, near_pole=0.02), 71)
+    d = o.DeviceInputs.from_host(inp)
+    full = o.sigma(d, precision, achstemp=True)
+    parts = [o.sigma(d.rows(*gd.row_range(37, r, 3)), precision, achstemp=True) for r in range(3)]
+    o.wait()
+    for key in ("achtemp", "asxtemp", "achstemp"):
+        total = sum(getattr(p_, key).cpu().numpy() for p_ in parts)
+        assert rel_err(total, getattr(full, key).cpu().numpy()) <= 1e-12, key

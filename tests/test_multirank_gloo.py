@@ -1,7 +1,7 @@
 """Host-side multi-rank logic with world_size 2 over gloo on the CPU: the
-slowest-rank timing, whole-job rate, rank-ordered partial sums of a sharded
-state (checked against the oracle), and a failing rank surfacing as an error
-on its peer instead of a hang."""
+slowest-rank timing, whole-job rate, rank-ordered partial sums of a state
+sharded by bands or by G' rows (checked against the oracle), and a failing
+rank surfacing as an error on its peer instead of a hang."""
 import datetime
 import os
 import socket
@@ -41,6 +41,15 @@ def _worker(rank, world, port, mode, out):
             a, b = (0, 4) if rank == 0 else (4, 8)
             part = oracle_py.run(inp, band_begin=a, band_end=b)["achtemp"]
             total = gd.sum_in_rank_order(part, dist)
+            if rank == 0:
+                out[0] = total
+        elif mode == "rows":
+            # One state, G' rows split across ranks as the reference's MPI
+            # version splits my_igp; partial sums added on rank 0.
+            inp = W.make_inputs(W.Shape(8, 2, 300, 11, 3), 6)
+            r0, r1 = gd.row_range(11, rank, world)
+            part = oracle_py.run(inp.rows(r0, r1))
+            total = [gd.sum_in_rank_order(part[k], dist) for k in ("achtemp", "asxtemp", "achstemp")]
             if rank == 0:
                 out[0] = total
         elif mode == "rank_fails":
@@ -91,6 +100,19 @@ def test_sharded_state_partials_add_up_in_rank_order():
     assert codes == [0, 0]
     want = oracle_py.run(W.make_inputs(W.Shape(8, 2, 300, 9, 3), 5))["achtemp"]
     np.testing.assert_allclose(out[0], want, rtol=1e-12)
+
+
+def test_row_sharded_state_adds_up_to_the_full_sums():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    from gppsigma import dist as gd, workload as W
+    assert [gd.row_range(11, r, 2) for r in (0, 1)] == [(0, 6), (6, 11)]
+    assert [gd.row_range(7, r, 3) for r in range(3)] == [(0, 2), (2, 4), (4, 7)]
+    out, codes = _run("rows")
+    assert codes == [0, 0]
+    want = oracle_py.run(W.make_inputs(W.Shape(8, 2, 300, 11, 3), 6))
+    for got, key in zip(out[0], ("achtemp", "asxtemp", "achstemp")):
+        np.testing.assert_allclose(got, want[key], rtol=1e-12)
 
 
 def test_failing_rank_surfaces_on_its_peer():
