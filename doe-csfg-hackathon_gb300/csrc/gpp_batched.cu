@@ -108,7 +108,7 @@ batched_fp64_kernel(const Problem *probs, const Partials *parts, const BatchItem
 // register-heavy) and unoccupied-band tiles (shared-memory pipeline) run as
 // two launches so each keeps its own occupancy.
 template <int NWC, int FRG>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, NWC <= 4 ? 3 : 2)
 batched_flag_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
                           const BatchItem *items, int n_items, int *head) {
     constexpr int KF = FRG * NWC * 4;
