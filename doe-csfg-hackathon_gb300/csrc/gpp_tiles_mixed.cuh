@@ -350,12 +350,12 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             const int k0 = c * KC;
             const int cnt = min(KC, nc - k0);
             if (chunk_mask & pole_mask) {
-#pragma unroll 1
+#pragma unroll 2
                 for (int il = lane; il < cnt; il += 32)
                     mixed_column<RNW, NWC, KC, true>(p, st, sb, il, k0 + il, row0, bandw,
                                                      band_end, iw0, wx, pole_thr, acc);
             } else {
-#pragma unroll 1
+#pragma unroll 2
                 for (int il = lane; il < cnt; il += 32)
                     mixed_column<RNW, NWC, KC, false>(p, st, sb, il, k0 + il, row0, bandw,
                                                       band_end, iw0, wx, pole_thr, acc);
