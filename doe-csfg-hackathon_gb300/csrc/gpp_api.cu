@@ -889,6 +889,17 @@ gpp_status gpp_last_kernel_ms(float *ms) {
     return GPP_OK;
 }
 
+gpp_status gpp_selftest_wait_timeout(int polls, gpp_stream_t stream) {
+    if (polls < 1 || polls > kWaitLimit) return fail(GPP_ERR_INVALID_ARGUMENT, "polls out of range");
+    int dev = 0;
+    int *err = nullptr;
+    gpp_status st = device_setup(&dev, &err);
+    if (st != GPP_OK) return st;
+    cudaError_t e = launch_wait_selftest(err, polls, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "wait self-test launch");
+    return GPP_OK;
+}
+
 gpp_status gpp_probe_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
     if (!fp64_tflops || !fp32_tflops) return fail(GPP_ERR_INVALID_ARGUMENT, "NULL output");
     cudaError_t e = probe_fma_peaks(fp64_tflops, fp32_tflops);

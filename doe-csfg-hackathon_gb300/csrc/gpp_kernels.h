@@ -70,6 +70,9 @@ cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *sp
                                 RowTiles rows = RowTiles());
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
                               cudaStream_t s, RowTiles rows = RowTiles());
+// One block that waits on an mbarrier nothing arrives at and records the
+// bounded-wait timeout in *err (exercises the failure path without a fault).
+cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t s);
 // Pipeline variants of the mixed kernel, selectable per call (autotuner).
 int mixed_variant_count();
 const char *mixed_variant_name(int variant);

@@ -265,6 +265,32 @@ cudaError_t launch_flag_mixed_t(const Problem &p, const Partials &part, const Sp
     return cudaGetLastError();
 }
 
+// Self-test of the bounded pipeline wait: one block waits on an mbarrier
+// that nothing arrives at, gives up after `polls` polls and records
+// kErrPipelineTimeout exactly as a tile does, then returns.
+__global__ void __launch_bounds__(32) wait_selftest_kernel(int *err, int polls) {
+    __shared__ unsigned long long bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    const bool ok = mbar_wait(&bar, 0u, &abort_flag, polls);
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        if (!ok) atomicOr(err, kErrPipelineTimeout);
+        mbar_inval(&bar);
+    }
+}
+
+cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t st) {
+    wait_selftest_kernel<<<1, 32, 0, st>>>(err, polls);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
                               cudaStream_t st, RowTiles rt) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;

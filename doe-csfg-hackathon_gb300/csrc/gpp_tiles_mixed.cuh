@@ -112,11 +112,11 @@ __device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 // Bounded wait for phase `parity` of `bar`.  Gives up (returns false) after
-// kWaitLimit polls, or as soon as another thread of the block has raised
+// `limit` polls, or as soon as another thread of the block has raised
 // *abort, so a block never spins without end.
 __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
-                                          volatile int *abort) {
-    for (int it = 0; it < kWaitLimit; ++it) {
+                                          volatile int *abort, int limit = kWaitLimit) {
+    for (int it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((it & 63) == 63 && *abort) return false;
     }

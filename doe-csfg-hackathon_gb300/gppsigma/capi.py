@@ -69,6 +69,7 @@ _SIGS = {
     "gpp_probe_fma_peaks": (_i, [C.POINTER(_d), C.POINTER(_d)]),
     "gpp_context_last_timing": (_i, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                      C.POINTER(C.c_float)]),
+    "gpp_selftest_wait_timeout": (_i, [_i, _vp]),
 }
 
 _lib = None

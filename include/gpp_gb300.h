@@ -252,6 +252,14 @@ gpp_status gpp_last_kernel_ms(float *ms);
  * TFLOP/s (FMA = 2 flops), from a short dependent-chain-free probe kernel. */
 gpp_status gpp_probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 
+/* No counterpart in the reference.  Failure-path self-test: launches one
+ * block on `stream` that waits on a shared-memory barrier nothing will
+ * complete, gives up after `polls` polls (1 .. 1<<22) exactly as the mixed
+ * kernels' pipeline waits do, and records the timeout in the device fault
+ * word.  The next gpp_wait on that stream returns GPP_ERR_DEVICE_TIMEOUT
+ * once; the context stays usable. */
+gpp_status gpp_selftest_wait_timeout(int polls, gpp_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
