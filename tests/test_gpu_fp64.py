@@ -1,6 +1,7 @@
 """FP64 CUDA path against the reference: golden fixtures produced by the
 reference's own functions, its README known answers, the reference-signature
 entry points, determinism, device-side fault reporting and the host path."""
+import dataclasses
 import os
 import subprocess
 
@@ -228,3 +229,22 @@ def test_row_shards_add_up_to_the_full_call(precision):
     for key in ("achtemp", "asxtemp", "achstemp"):
         total = sum(getattr(p_, key).cpu().numpy() for p_ in parts)
         assert rel_err(total, getattr(full, key).cpu().numpy()) <= 1e-12, key
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_indinv_remaps_the_clamped_igp(precision):
+    """A non-identity indinv (GPPComplex.h:304) remaps igp = indinv[min(inv_igp_index,
+    ncouls-1)]: the same bits as the identity indinv with that map folded into
+    inv_igp_index."""
+    o = ops()
+    shape = W.Shape(12, 2, 800, 21, 3, near_pole=0.02, igp_overflow=3)
+    inp = W.make_inputs(shape, 91)
+    perm = np.random.default_rng(3).permutation(shape.ncouls).astype(np.int32)
+    a_in = dataclasses.replace(inp, indinv=perm)
+    folded = perm[np.minimum(inp.inv_igp_index, shape.ncouls - 1)].astype(np.int32)
+    b_in = dataclasses.replace(inp, inv_igp_index=folded)
+    a = o.sigma(o.DeviceInputs.from_host(a_in), precision, acht_n1=True, achstemp=True)
+    b = o.sigma(o.DeviceInputs.from_host(b_in), precision, acht_n1=True, achstemp=True)
+    o.wait()
+    for key in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
+        assert torch.equal(torch.view_as_real(getattr(a, key)), torch.view_as_real(getattr(b, key))), key
