@@ -21,6 +21,7 @@ namespace {
 thread_local std::string t_err;
 thread_local unsigned long long t_launches = 0;
 thread_local cudaStream_t t_compat_stream = nullptr;
+thread_local int t_dropin_precision = -1;  // -1: the process default
 thread_local bool t_timing = false;
 thread_local cudaEvent_t t_ev0 = nullptr, t_ev1 = nullptr;
 thread_local bool t_timed = false;
@@ -205,6 +206,17 @@ struct SideStream {
     cudaEvent_t fork = nullptr, join = nullptr;
 };
 thread_local SideStream t_side;
+
+// Precision of the drop-in entry points: gpp_set_dropin_precision on this
+// thread, else GPP_DROPIN_PRECISION=mixed|fp64 in the environment, else FP64.
+int dropin_precision() {
+    if (t_dropin_precision >= 0) return t_dropin_precision;
+    static const int env = [] {
+        const char *v = getenv("GPP_DROPIN_PRECISION");
+        return (v && strcmp(v, "mixed") == 0) ? (int)GPP_PRECISION_MIXED : (int)GPP_PRECISION_FP64;
+    }();
+    return env;
+}
 
 // Whether the mixed path runs the occupied-band kernel concurrently on the
 // side stream (GPP_OVERLAP_OCCUPIED=1) or before the unoccupied-band kernel
@@ -406,6 +418,14 @@ gpp_status gpp_set_stream(gpp_stream_t stream) {
 }
 gpp_stream_t gpp_get_stream(void) { return reinterpret_cast<gpp_stream_t>(t_compat_stream); }
 
+gpp_status gpp_set_dropin_precision(int precision) {
+    if (precision != -1 && precision != GPP_PRECISION_FP64 && precision != GPP_PRECISION_MIXED)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
+    t_dropin_precision = precision;
+    return GPP_OK;
+}
+int gpp_get_dropin_precision(void) { return dropin_precision(); }
+
 }  // extern "C"
 
 namespace {
@@ -465,7 +485,7 @@ gpp_status gpp_kernel_gpu(const gpp_complex *wtilde_array, const gpp_complex *aq
     q.wx_stride = 0;
     q.occ = 1.0;
     q.semantics = GPP_SEM_COMPLEX_SEQ;
-    q.precision = GPP_PRECISION_FP64;
+    q.precision = dropin_precision();
     gpp_status st = validate(&q);
     if (st != GPP_OK) return st;
     if (!achtemp_re || !achtemp_im) return fail(GPP_ERR_INVALID_ARGUMENT, "achtemp_re/im is NULL");
@@ -473,7 +493,7 @@ gpp_status gpp_kernel_gpu(const gpp_complex *wtilde_array, const gpp_complex *aq
     o.ach_re = achtemp_re;
     o.ach_im = achtemp_im;
     o.accumulate = 1;
-    return run_sigma(to_problem(q), 0, number_bands, GPP_PRECISION_FP64, o, true, t_compat_stream);
+    return run_sigma(to_problem(q), 0, number_bands, q.precision, o, true, t_compat_stream);
 }
 
 static gpp_problem compat_problem(int number_bands, int nvband, int ngpown, int ncouls,
@@ -497,7 +517,7 @@ static gpp_problem compat_problem(int number_bands, int nvband, int ngpown, int 
     q.wx_stride = 0;
     q.occ = occ;
     q.semantics = GPP_SEM_COMPLEX_SEQ;
-    q.precision = GPP_PRECISION_FP64;
+    q.precision = dropin_precision();
     return q;
 }
 
@@ -519,7 +539,7 @@ gpp_status gpp_till_nvband(int nvband, int ngpown, int ncouls, const int *inv_ig
     o.asx = reinterpret_cast<double2 *>(asxtemp);
     o.n1 = reinterpret_cast<double2 *>(acht_n1_loc);
     o.accumulate = 1;
-    return run_sigma(to_problem(q), 0, nvband, GPP_PRECISION_FP64, o, true, t_compat_stream);
+    return run_sigma(to_problem(q), 0, nvband, q.precision, o, true, t_compat_stream);
 }
 
 gpp_status gpp_noflag_occ_solver(int number_bands, int nvband, int ngpown, int ncouls,
@@ -538,8 +558,7 @@ gpp_status gpp_noflag_occ_solver(int number_bands, int nvband, int ngpown, int n
     o.ach_im = achtemp_im;
     o.n1 = reinterpret_cast<double2 *>(acht_n1_loc);
     o.accumulate = 1;
-    return run_sigma(to_problem(q), nvband, number_bands, GPP_PRECISION_FP64, o, true,
-                     t_compat_stream);
+    return run_sigma(to_problem(q), nvband, number_bands, q.precision, o, true, t_compat_stream);
 }
 
 static gpp_status reduce_achstemp_impl(int number_bands, const int *inv_igp_index, int ncouls,

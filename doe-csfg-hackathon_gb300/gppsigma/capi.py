@@ -70,6 +70,8 @@ _SIGS = {
     "gpp_context_last_timing": (_i, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                      C.POINTER(C.c_float)]),
     "gpp_selftest_wait_timeout": (_i, [_i, _vp]),
+    "gpp_set_dropin_precision": (_i, [_i]),
+    "gpp_get_dropin_precision": (_i, []),
 }
 
 _lib = None

@@ -69,7 +69,8 @@ typedef enum gpp_semantics {
  * Drop-in entry points with the reference's argument lists.
  * They take the stream set by gpp_set_stream() (default: legacy stream),
  * use the band-independent wx_array[nend-nstart] of the reference, the
- * GPP_SEM_COMPLEX_SEQ semantics of GPPComplex.cu, FP64 arithmetic, and ADD
+ * GPP_SEM_COMPLEX_SEQ semantics of GPPComplex.cu, FP64 arithmetic (unless
+ * gpp_set_dropin_precision below selects mixed), and ADD
  * into the caller's output arrays (the reference accumulates with atomics
  * into caller-zeroed arrays, gppCudaVer.cpp:360-361,376-377).
  * ------------------------------------------------------------------------ */
@@ -119,6 +120,17 @@ gpp_status gpp_reduce_achstemp(int number_bands, const int *inv_igp_index, int n
 /* Stream used by the drop-in entry points above (per host thread). */
 gpp_status gpp_set_stream(gpp_stream_t stream);
 gpp_stream_t gpp_get_stream(void);
+
+/* No counterpart in the reference.  Arithmetic of the drop-in entry points
+ * above except gpp_reduce_achstemp (per host thread): GPP_PRECISION_FP64
+ * (the reference's) or GPP_PRECISION_MIXED (float-float, <= 1e-8 of FP64,
+ * several times faster); -1 restores the process default, which is
+ * GPP_PRECISION_MIXED when the environment has GPP_DROPIN_PRECISION=mixed
+ * and GPP_PRECISION_FP64 otherwise -- so an unmodified reference driver can
+ * run the mixed kernels.  gpp_get_dropin_precision returns the value in
+ * effect. */
+gpp_status gpp_set_dropin_precision(int precision);
+int gpp_get_dropin_precision(void);
 
 /* ------------------------------------------------------------------------
  * Full problem API: occupied and unoccupied bands in one call, per-band

@@ -248,3 +248,22 @@ def test_indinv_remaps_the_clamped_igp(precision):
     o.wait()
     for key in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
         assert torch.equal(torch.view_as_real(getattr(a, key)), torch.view_as_real(getattr(b, key))), key
+
+
+def test_unmodified_reference_driver_runs_mixed_from_the_environment():
+    """GPP_DROPIN_PRECISION=mixed makes the reference's own call sequence
+    (gpp_driver.ex) use the float-float kernels: the README known answer
+    within 1e-8."""
+    build.build()
+    env = dict(os.environ, GPP_DROPIN_PRECISION="mixed")
+    out = subprocess.run([build.DRIVER, "512", "2", "800", "20"], capture_output=True, text=True,
+                         timeout=120, env=env)
+    assert out.returncode == 0, out.stderr
+    case = next(c for c in CASES if c["name"] == "ramp_512_2_800_20")
+    got = []
+    for line in out.stdout.splitlines():
+        if line.startswith("achtemp["):
+            re_s, im_s = line.split("= (")[1].rstrip(")").split(",")
+            got.append(complex(float(re_s), float(im_s)))
+    assert len(got) == 3
+    assert rel_err(got, unhex(case["achtemp"])) <= 1e-8

@@ -168,3 +168,47 @@ def test_true_error_of_both_paths(shape, mixed_tol):
     print("error against the extended-precision oracle:", errs)
     assert errs["fp64"] <= 1e-12
     assert errs["mixed"] <= mixed_tol
+
+
+def test_dropin_entry_points_run_mixed_when_asked():
+    """gpp_set_dropin_precision(MIXED): the reference-signature entry points
+    (d_till_nvband, d_noFlagOCCSolver, gppKernelGPU) run the float-float
+    kernels -- different bits, within 1e-8 of their FP64 results."""
+    o = ops()
+    lib = capi.load()
+    inp = W.make_inputs(W.Shape(10, 3, 700, 11, 3, near_pole=0.05), 33)
+    inp.wx_array = inp.wx_array[:1].copy()  # band-independent wx, as the reference
+    d = o.DeviceInputs.from_host(inp)
+    s = inp.shape
+
+    def run():
+        re_ = torch.zeros(3, dtype=torch.float64, device="cuda")
+        im_ = torch.zeros(3, dtype=torch.float64, device="cuda")
+        asx = torch.zeros(3, dtype=torch.complex128, device="cuda")
+        n1 = torch.zeros(s.number_bands, dtype=torch.complex128, device="cuda")
+        o.d_till_nvband(s.nvband, s.ngpown, s.ncouls, d.inv_igp_index, d.wx_array, d.wtilde_array,
+                        d.aqsmtemp, d.aqsntemp, d.I_eps_array, asx, d.vcoul, n1, re_, im_, 1.0)
+        o.d_noFlagOCCSolver(s.number_bands, s.nvband, s.ngpown, s.ncouls, d.inv_igp_index,
+                            d.wx_array, d.wtilde_array, d.aqsmtemp, d.aqsntemp, d.I_eps_array,
+                            d.vcoul, re_, im_, n1)
+        re0 = torch.zeros(3, dtype=torch.float64, device="cuda")
+        im0 = torch.zeros(3, dtype=torch.float64, device="cuda")
+        o.gppKernelGPU(d.wtilde_array, d.aqsntemp, d.aqsmtemp, d.I_eps_array, s.ncouls, s.ngpown,
+                       s.number_bands, d.wx_array, re0, im0, d.vcoul, 0, 3, d.indinv,
+                       d.inv_igp_index)
+        o.wait()
+        return [(re_ + 1j * im_).cpu().numpy(), asx.cpu().numpy(), (re0 + 1j * im0).cpu().numpy()]
+
+    assert lib.gpp_get_dropin_precision() == capi.PRECISION["fp64"]
+    ref = run()
+    try:
+        capi.check(lib.gpp_set_dropin_precision(capi.PRECISION["mixed"]), "set precision")
+        assert lib.gpp_get_dropin_precision() == capi.PRECISION["mixed"]
+        got = run()
+    finally:
+        capi.check(lib.gpp_set_dropin_precision(-1), "reset precision")
+    assert lib.gpp_get_dropin_precision() == capi.PRECISION["fp64"]
+    assert lib.gpp_set_dropin_precision(7) == capi.GPP_ERR_INVALID_ARGUMENT
+    for g, w in zip(got, ref):
+        assert rel_err(g, w) <= MIXED_TOL
+    assert not np.array_equal(got[0], ref[0])  # the mixed kernels really ran
