@@ -135,8 +135,18 @@ batched_flag_mixed_kernel(const Problem *probs, const Partials *parts, const Spl
     }
 }
 
+// Columns per pipeline chunk of the persistent mixed kernel: the fastest
+// block-sync chunk of the single-state kernel measured on GB300 (192 columns
+// for up to 4 frequencies, 256 for the 8-frequency tile).
+template <int NWC>
+__host__ __device__ constexpr int batch_kc() { return NWC <= 4 ? 192 : 256; }
+
+// Resident blocks as the single-state kernel: 4 (128 registers) up to 4
+// frequencies, 3 (168 registers) for the 8-frequency tile.  Left to the
+// compiler's heuristic, the persistent loop takes 158 and 254 registers and
+// a quarter to a third of the warps.
 template <int RG, int NWC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, NWC <= 4 ? 4 : 3)
 batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
                             const BatchItem *items, int n_items, int *head) {
     __shared__ int s_item;
@@ -151,9 +161,8 @@ batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const S
         const Problem p = probs[bi.state];
         const Partials part = parts[bi.state];
         const SplitPlanes sp = splits[bi.state];
-        if (!mixed_tile<1, RG, NWC, 4, 128, 2, kSyncBlock>(p, part, sp, p.nv, p.nb, bi.row_tile,
-                                                           bi.band_tile, bi.iw_chunk, bi.tile,
-                                                           reinit))
+        if (!mixed_tile<1, RG, NWC, 4, batch_kc<NWC>(), 2, kSyncBlock>(
+                p, part, sp, p.nv, p.nb, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, reinit))
             return;  // abandoned after a bounded wait; the fault bit is set
         reinit = true;
         __syncthreads();
@@ -463,7 +472,7 @@ cudaError_t prepare_persistent(gpp_batch *b) {
     if (b->precision == GPP_PRECISION_MIXED) {
         constexpr int RG = 2;  // one row pair of the split planes
         auto kern = batched_noflag_mixed_kernel<RG, NWC>;
-        b->smem = sizeof(float4) * 2 * (2 * RG + 4) * 128;
+        b->smem = sizeof(float4) * 2 * (2 * RG + 4) * batch_kc<NWC>();
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)b->smem);
         if (e != cudaSuccess) return e;
