@@ -649,7 +649,12 @@ struct gpp_context {
     bool timed = false;
 };
 
-constexpr int kHostRowPieces = 8;
+// Row pieces of the host path, in sixteenths of the row pairs: a small first
+// piece so the kernels start early, then larger ones.  Each piece is copied
+// while the previous ones compute (the link moves rows ~25x faster than the
+// kernels consume them), and fewer pieces mean fewer partial last waves of
+// the unoccupied-band kernel.
+constexpr int kHostPieceCuts[] = {1, 5, 16};
 
 static void context_release(gpp_context *c) {
     for (auto &e : c->ev)
@@ -737,8 +742,13 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     GPP_CUDA_TRY(cudaEventRecord(ctx->bands_ready, ctx->copy), "cudaEventRecord");
     RowPieces pieces;
     const int pairs = (int)((ng + 1) / 2);
-    pieces.n = pairs < kHostRowPieces ? (pairs > 0 ? pairs : 1) : kHostRowPieces;
-    for (int k = 0; k <= pieces.n; ++k) pieces.pair[k] = (int)((long long)pairs * k / pieces.n);
+    pieces.n = 0;
+    pieces.pair[0] = 0;
+    for (int cut : kHostPieceCuts) {
+        const int b = (int)((long long)pairs * cut / 16);
+        if (b > pieces.pair[pieces.n]) pieces.pair[++pieces.n] = b;
+    }
+    if (pieces.n == 0) pieces.pair[++pieces.n] = 0;  // no rows: one empty piece
     for (int k = 0; k < pieces.n; ++k) {
         const size_t r0 = 2 * (size_t)pieces.pair[k];
         const size_t r1 = std::min(2 * (size_t)pieces.pair[k + 1], ng);
