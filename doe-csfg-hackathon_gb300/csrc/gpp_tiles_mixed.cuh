@@ -434,7 +434,12 @@ __device__ __forceinline__ bool df_gt(df a, df t) {
     const df e = df_norm(df_sub(a, t));
     return e.h > 0.f || (e.h == 0.f && e.l > 0.f);
 }
-__device__ __forceinline__ df df_of(double x) { return split(x); }
+// The solver's thresholds (limittwo, limitone, to1) as float-float values,
+// rounded at compile time: converted on the device, the compiler may
+// recompute them (FP64 conversions) inside the term loop.
+constexpr float kLim2H = (float)kLimitTwo, kLim2L = (float)(kLimitTwo - (double)kLim2H);
+constexpr float kLim1H = (float)kLimitOne, kLim1L = (float)(kLimitOne - (double)kLim1H);
+constexpr float kTo1H = (float)kTo1, kTo1L = (float)(kTo1 - (double)kTo1H);
 __device__ __forceinline__ df df_abs2(df re, df im) { return df_add(df_sqr(re), df_sqr(im)); }
 // (a.re + i a.im) * (b.re + i b.im) in df.
 __device__ __forceinline__ void df_cmul(df ar, df ai, df br, df bi, df &cr, df &ci) {
@@ -465,13 +470,14 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
     const int row0 = row_tile * RG;
     const int iw0 = iw_chunk * NWC;
     const int nc = p.nc;
-    const df kLim2 = df_of(kLimitTwo), kLim1 = df_of(kLimitOne), kT1 = df_of(kTo1);
+    const df kLim2 = {kLim2H, kLim2L}, kLim1 = {kLim1H, kLim1L}, kT1 = {kTo1H, kTo1L};
 
     const float4 *rp = s.rows + (size_t)row_tile * 4 * nc;  // this row pair's planes
     const float4 *bp = s.band + (size_t)band * nc;
     df wx[NWC], cwr2[NWC];
     double wx64[NWC], cwr[NWC];
     float thr[NWC];
+    bool cut_on[NWC];  // the ssx cutoff applies (COMPLEX_SEQ, wx < 0); no FP64 test per term
 #pragma unroll
     for (int w = 0; w < NWC; ++w) {
         wx64[w] = __ldg(p.wx + (size_t)band * p.wx_stride + min(iw0 + w, p.nw - 1));
@@ -480,6 +486,7 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
         cwr[w] = c / (c * c);  // wx^2 / pow(wx^2, 2) (gppComplex_seq.cpp:38-41)
         cwr2[w] = split(cwr[w] * cwr[w]);
         thr[w] = 1e-6f * wx[w].h * wx[w].h;
+        cut_on[w] = SEM == kSemComplexSeq && wx64[w] < 0.0;
     }
     // Accumulators: aqsn*sch, sum of aqsn*Omega2 over branch-A terms (times
     // 1/wx^2 later), aqsn*ssx of branch-B and pole terms.
@@ -540,8 +547,7 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
                     const df tim = df_mul(df_add(df_mul(Ai, wr), Ar_wti), rden);
                     as_r[g][w] = df_add(as_r[g][w], tre);
                     as_i[g][w] = df_add(as_i[g][w], tim);
-                    const bool cut = SEM == kSemComplexSeq && wx64[w] < 0.0 &&
-                                     df_gt(df_mul(om_wt, cwr2[w]), cut_rhs);
+                    const bool cut = cut_on[w] && df_gt(df_mul(om_wt, cwr2[w]), cut_rhs);
                     if (!cut) {
                         xa_r[g][w] = df_add(xa_r[g][w], Br);
                         xa_i[g][w] = df_add(xa_i[g][w], Bi);
@@ -563,8 +569,8 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
                     df_cmul(tr, ti, df_mul(dr, r2), df_mul(di, r2), sr, si);
                     sr = df{-sr.h, -sr.l};
                     si = df{-si.h, -si.l};
-                    const bool cut = SEM == kSemComplexSeq && wx64[w] < 0.0 &&
-                                     df_gt(df_mul(df_abs2(sr, si), awt2), cut_rhs);
+                    const bool cut =
+                        cut_on[w] && df_gt(df_mul(df_abs2(sr, si), awt2), cut_rhs);
                     if (!cut) {
                         df pr, pi;
                         df_cmul(ar, ai, sr, si, pr, pi);
