@@ -10,6 +10,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 namespace gpp {
 
 struct df {
@@ -104,5 +106,38 @@ __host__ __device__ __forceinline__ df split(double x) {
 #endif
 }
 __host__ __device__ __forceinline__ double to_double(df a) { return (double)a.h + (double)a.l; }
+
+// split(x) from the bits of x with integer operations, for the prep kernels
+// that split gigabytes of inputs: on GB300 the FP64 conversions and the
+// subtraction of split() run on the narrow FP64 pipe.  With x = (2^52 + m)
+// 2^(e-1075): h keeps the top 23 bits of m, rounded to nearest even on the
+// low 29; x - h = r 2^(e-1075) exactly, with r the signed remainder
+// (|r| <= 2^28), and l = fl(r) 2^(e-1075): one integer-to-float rounding,
+// then an exact scaling.  Same bits as split() wherever h and the scaled l
+// are normal floats; exponents outside [2^-60, 2^48] (zero, subnormal, huge,
+// Inf, NaN) take split().
+__host__ __device__ __forceinline__ df split_bits(double x) {
+    unsigned long long b;
+    memcpy(&b, &x, 8);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 60 || e > 1023 + 48) return split(x);
+    const unsigned mhi = (unsigned)(b >> 29) & 0x7fffffu;  // mantissa bits 51..29
+    const unsigned rem = (unsigned)b & 0x1fffffffu;         // mantissa bits 28..0
+    const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (mhi & 1u))) ? 1u : 0u;
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    // A carry out of the mantissa moves h to the next binade, as rounding does.
+    const unsigned hb = sign | ((((unsigned)(e - 1023 + 127) << 23) | mhi) + up);
+    const int r = (int)rem - (int)(up << 29);
+    const unsigned sb = (unsigned)(e - 1075 + 127) << 23;    // 2^(e-1075), a normal float
+    float h, scale;
+    memcpy(&h, &hb, 4);
+    memcpy(&scale, &sb, 4);
+#ifdef __CUDA_ARCH__
+    const float l = __fmul_rn(__int2float_rn(r), scale);
+#else
+    const float l = (float)r * scale;
+#endif
+    return {h, (sign && r != 0) ? -l : l};  // +0 for an exact x, as split() gives
+}
 
 }  // namespace gpp

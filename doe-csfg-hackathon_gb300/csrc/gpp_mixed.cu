@@ -49,36 +49,43 @@ size_t mask_words(const Problem &p) {
 }
 
 // One thread per (row pair, ig): Q = wtilde * I_eps in FP64 for both rows,
-// then the hi/lo splits interleaved by row (the row-pair plane layout).
+// then the hi/lo splits (split_bits: integer operations, off the FP64 pipe)
+// interleaved by row (the row-pair plane layout).  Blocks cover 256 columns
+// of one row pair at a time (grid x over columns, y over row pairs).
 // The same pass sets the row pairs' value-bucket masks: lanes that share a
 // mask word OR their bits together and one of them updates the word (the
 // result does not depend on the order).
 __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes s, int pair0,
                                                          int pair1) {
     const size_t nc = (size_t)p.nc;
-    const size_t n = (size_t)(pair1 - pair0) * nc;
     const size_t nmw = (nc + kMaskCols - 1) / kMaskCols;
-    for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
-        const size_t j = pair0 + i / nc, ig = i % nc;
+    for (int jj = pair0 + blockIdx.y; jj < pair1; jj += gridDim.y) {
+        const size_t j = (size_t)jj;
         const size_t r0 = 2 * j, r1 = min(2 * j + 1, (size_t)p.ng - 1);
-        const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
-        const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
-        const double2 q1 = cmul(wt1, __ldg(p.ieps + r1 * nc + ig));
-        const df a0 = split(wt0.x), a1 = split(wt1.x), b0 = split(wt0.y), b1 = split(wt1.y);
-        const df c0 = split(q0.x), c1 = split(q1.x), d0 = split(q0.y), d1 = split(q1.y);
-        float4 *o = s.rows + j * 4 * nc + ig;
-        o[0] = make_float4(a0.h, a1.h, a0.l, a1.l);
-        o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
-        o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
-        o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
-        const unsigned long long bits = bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
-        const unsigned long long word = j * nmw + ig / kMaskCols;
-        const unsigned act = __activemask();
-        const unsigned grp = __match_any_sync(act, word);
-        const unsigned lo = __reduce_or_sync(grp, (unsigned)bits);
-        const unsigned hi = __reduce_or_sync(grp, (unsigned)(bits >> 32));
-        if ((int)(threadIdx.x & 31) == __ffs(grp) - 1)
-            atomicOr(s.masks + word, ((unsigned long long)hi << 32) | lo);
+        for (size_t ig = (size_t)blockIdx.x * 256 + threadIdx.x; ig < nc;
+             ig += (size_t)gridDim.x * 256) {
+            const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
+            const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
+            const double2 q1 = cmul(wt1, __ldg(p.ieps + r1 * nc + ig));
+            const df a0 = split_bits(wt0.x), a1 = split_bits(wt1.x);
+            const df b0 = split_bits(wt0.y), b1 = split_bits(wt1.y);
+            const df c0 = split_bits(q0.x), c1 = split_bits(q1.x);
+            const df d0 = split_bits(q0.y), d1 = split_bits(q1.y);
+            float4 *o = s.rows + j * 4 * nc + ig;
+            o[0] = make_float4(a0.h, a1.h, a0.l, a1.l);
+            o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
+            o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
+            o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
+            const unsigned long long bits =
+                bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
+            const unsigned long long word = j * nmw + ig / kMaskCols;
+            const unsigned act = __activemask();
+            const unsigned grp = __match_any_sync(act, word);
+            const unsigned lo = __reduce_or_sync(grp, (unsigned)bits);
+            const unsigned hi = __reduce_or_sync(grp, (unsigned)(bits >> 32));
+            if ((int)(threadIdx.x & 31) == __ffs(grp) - 1)
+                atomicOr(s.masks + word, ((unsigned long long)hi << 32) | lo);
+        }
     }
 }
 
@@ -88,7 +95,7 @@ __global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes
     const size_t base = (size_t)b0 * p.nc;
     for (size_t i = (size_t)blockIdx.x * 256 + threadIdx.x; i < n; i += (size_t)gridDim.x * 256) {
         const double2 a = __ldg(p.aqsn + base + i);
-        const df ar = split(a.x), ai = split(a.y);
+        const df ar = split_bits(a.x), ai = split_bits(a.y);
         s.band[base + i] = make_float4(ar.h, ar.l, ai.h, ai.l);
     }
     const int nwx = (b1 - b0) * p.nw;
@@ -229,7 +236,11 @@ cudaError_t launch_split_bands(const Problem &p, void *split_ws, int b0, int b1,
 cudaError_t launch_split_rows(const Problem &p, void *split_ws, RowTiles pairs, cudaStream_t st) {
     const RowTiles r = pairs.clip((p.ng + 1) / 2);
     if (r.end <= r.begin) return cudaSuccess;
-    split_rows_kernel<<<split_blocks(), 256, 0, st>>>(p, planes(p, split_ws), r.begin, r.end);
+    // Columns: up to 64 blocks of 256 per row pair; row pairs: enough blocks
+    // in y for ~8 per SM in all.
+    const int bx = std::min(64, std::max(1, ceil_div(p.nc, 256)));
+    const int by = std::min(r.end - r.begin, std::max(1, split_blocks() / bx));
+    split_rows_kernel<<<dim3(bx, by), 256, 0, st>>>(p, planes(p, split_ws), r.begin, r.end);
     count_launch();
     return cudaGetLastError();
 }
