@@ -107,13 +107,22 @@ __host__ __device__ __forceinline__ df split(double x) {
 }
 __host__ __device__ __forceinline__ double to_double(df a) { return (double)a.h + (double)a.l; }
 
-// split(x) from the bits of x with integer operations, for the prep kernels
-// that split gigabytes of inputs: on GB300 the FP64 conversions and the
-// subtraction of split() run on the narrow FP64 pipe.  With x = (2^52 + m)
-// 2^(e-1075): h keeps the top 23 bits of m, rounded to nearest even on the
-// low 29; x - h = r 2^(e-1075) exactly, with r the signed remainder
-// (|r| <= 2^28), and l = fl(r) 2^(e-1075): one integer-to-float rounding,
-// then an exact scaling.  Same bits as split() wherever h and the scaled l
+// Small integer k (|k| < 2^22) to float, exactly, without a conversion
+// instruction: 1.5 * 2^23 + k has k in its low mantissa bits.
+__host__ __device__ __forceinline__ float small_int_to_float(int k) {
+    const unsigned u = 0x4B400000u + (unsigned)k;
+    float f;
+    memcpy(&f, &u, 4);
+    return fsub(f, 12582912.0f);
+}
+// split(x) from the bits of x with integer and FP32 operations, for the prep
+// kernels that split gigabytes of inputs: on GB300 the FP64 conversions and
+// subtraction of split(), and integer-to-float conversions too, run on the
+// narrow FP64 pipe.  With x = (2^52 + m) 2^(e-1075): h keeps the top 23 bits
+// of m, rounded to nearest even on the low 29; x - h = r 2^(e-1075) exactly,
+// with r the signed remainder (|r| <= 2^28).  Writing r = rh 2^14 + rl, both
+// parts exact floats, l = fma(rh, 2^(e-1061), rl 2^(e-1075)) rounds r
+// 2^(e-1075) once, as split() does.  Same bits as split() wherever h and l
 // are normal floats; exponents outside [2^-60, 2^48] (zero, subnormal, huge,
 // Inf, NaN) take split().
 __host__ __device__ __forceinline__ df split_bits(double x) {
@@ -128,15 +137,14 @@ __host__ __device__ __forceinline__ df split_bits(double x) {
     // A carry out of the mantissa moves h to the next binade, as rounding does.
     const unsigned hb = sign | ((((unsigned)(e - 1023 + 127) << 23) | mhi) + up);
     const int r = (int)rem - (int)(up << 29);
-    const unsigned sb = (unsigned)(e - 1075 + 127) << 23;    // 2^(e-1075), a normal float
-    float h, scale;
+    const float rh = small_int_to_float(r >> 14), rl = small_int_to_float(r & 0x3fff);
+    const unsigned sb = (unsigned)(e - 1075 + 127) << 23;  // 2^(e-1075), a normal float
+    const unsigned sb14 = sb + (14u << 23);                // 2^(e-1061)
+    float h, scale, scale14;
     memcpy(&h, &hb, 4);
     memcpy(&scale, &sb, 4);
-#ifdef __CUDA_ARCH__
-    const float l = __fmul_rn(__int2float_rn(r), scale);
-#else
-    const float l = (float)r * scale;
-#endif
+    memcpy(&scale14, &sb14, 4);
+    const float l = fmaf(rh, scale14, fmul(rl, scale));
     return {h, (sign && r != 0) ? -l : l};  // +0 for an exact x, as split() gives
 }
 
