@@ -125,11 +125,22 @@ __host__ __device__ __forceinline__ float small_int_to_float(int k) {
 // 2^(e-1075) once, as split() does.  Same bits as split() wherever h and l
 // are normal floats; exponents outside [2^-60, 2^48] (zero, subnormal, huge,
 // Inf, NaN) take split().
+// The out-of-range case, kept out of line so that the compiler cannot
+// hoist its FP64 conversions into the common path.
+#ifdef __CUDA_ARCH__
+__device__ __noinline__ df split_far(double x) { return split(x); }
+#else
+inline df split_far(double x) { return split(x); }
+#endif
 __host__ __device__ __forceinline__ df split_bits(double x) {
     unsigned long long b;
+#ifdef __CUDA_ARCH__
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));  // opaque: no FP compare for the range test
+#else
     memcpy(&b, &x, 8);
+#endif
     const int e = (int)((b >> 52) & 0x7ff);
-    if (e < 1023 - 60 || e > 1023 + 48) return split(x);
+    if (e < 1023 - 60 || e > 1023 + 48) return split_far(x);
     const unsigned mhi = (unsigned)(b >> 29) & 0x7fffffu;  // mantissa bits 51..29
     const unsigned rem = (unsigned)b & 0x1fffffffu;         // mantissa bits 28..0
     const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (mhi & 1u))) ? 1u : 0u;
