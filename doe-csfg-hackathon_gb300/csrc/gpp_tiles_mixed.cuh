@@ -448,6 +448,25 @@ __device__ __forceinline__ void df_cmul(df ar, df ai, df br, df bi, df &cr, df &
 }
 __device__ __forceinline__ df df_scale(df a, float k) { return {fmul(a.h, k), fmul(a.l, k)}; }
 
+// An occupied-band term near the pole, in FP64 from the original inputs,
+// split to float-float: aqsn*sch (sr, si) and aqsn*ssx (xr, xi).  Out of line:
+// inlined, its FP64 code took registers from the float-float term loop.
+struct FlagPole {
+    df sr, si, xr, xi;
+};
+template <int SEM>
+static __device__ __noinline__ FlagPole flag_pole(const Problem &p, int row, int band, int ig,
+                                                  double wx, double cwr) {
+    const size_t nc = (size_t)p.nc;
+    const double2 wt = __ldg(p.wt + (size_t)row * nc + ig);
+    const double2 ie = __ldg(p.ieps + (size_t)row * nc + ig);
+    const double2 a = __ldg(p.aqsn + (size_t)band * nc + ig);
+    const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
+    double2 s64 = make_double2(0.0, 0.0), x64 = make_double2(0.0, 0.0);
+    flag_term<SEM>(wx, cwr, wt, wt2, cmul(wt2, ie), ie, a, s64, x64);
+    return {split(s64.x), split(s64.y), split(x64.x), split(x64.y)};
+}
+
 // One occupied-band tile in mixed precision: rows row_tile*RG.., one band,
 // frequencies iw_chunk*NWC..; reads the float-float split planes (bands
 // [0, nvband) must have been split too).  Per term, on df values:
@@ -526,17 +545,12 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
                 const df d = df_add(df_sqr(wr), wti2);       // |wdiff|^2
                 if (d.h < thr[w]) {
                     // Near the pole: the whole term in FP64 from the inputs.
-                    const int row = min(row0 + g, p.ng - 1);
-                    const double2 wt = __ldg(p.wt + (size_t)row * nc + ig);
-                    const double2 ie = __ldg(p.ieps + (size_t)row * nc + ig);
-                    const double2 a = __ldg(p.aqsn + (size_t)band * nc + ig);
-                    const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
-                    double2 s64 = make_double2(0.0, 0.0), x64 = make_double2(0.0, 0.0);
-                    flag_term<SEM>(wx64[w], cwr[w], wt, wt2, cmul(wt2, ie), ie, a, s64, x64);
-                    as_r[g][w] = df_add(as_r[g][w], split(s64.x));
-                    as_i[g][w] = df_add(as_i[g][w], split(s64.y));
-                    xb_r[g][w] = df_add(xb_r[g][w], split(x64.x));
-                    xb_i[g][w] = df_add(xb_i[g][w], split(x64.y));
+                    const FlagPole t = flag_pole<SEM>(p, min(row0 + g, p.ng - 1), band, ig,
+                                                      wx64[w], cwr[w]);
+                    as_r[g][w] = df_add(as_r[g][w], t.sr);
+                    as_i[g][w] = df_add(as_i[g][w], t.si);
+                    xb_r[g][w] = df_add(xb_r[g][w], t.xr);
+                    xb_i[g][w] = df_add(xb_i[g][w], t.xi);
                     continue;
                 }
                 const df rden = df_rcp(d);
