@@ -12,6 +12,10 @@ Two products:
     - ``libref_kerseq.so``:      gppKerSeq.cpp      + ref_harness.cpp
     - ``gppKerSeq.ex``, ``gppComplex_seq.ex``, ``gppOpenMP3.ex``: the
       unmodified reference executables (README known-answer runs, CPU timing).
+    - ``GPPComplex.cubin``: the device code of the reference's own CUDA
+      version (GPPComplex.cu) for sm_103a, loaded by oracle/ref_gpu.py to
+      time the reference's GPU kernels beside the new ones.  Device code has
+      no host architecture, so it runs on the GPU host as built here.
   The reference's main() is renamed with -Dmain=... in the library builds.
 """
 from __future__ import annotations
@@ -79,6 +83,25 @@ def build_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool
         srcp = os.path.join(ref_dir, src)
         if force or _stale(target, [srcp]):
             _run(["g++", "-O3", "-w", "-I", ref_dir] + extra + [srcp, "-o", target])
+    build_reference_cubin(ref_dir, force)
+    return True
+
+
+def build_reference_cubin(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool:
+    """Compile GPPComplex.cu's kernels (device code only) into
+    oracle/_ref/GPPComplex.cubin; False without the sources or nvcc."""
+    src = os.path.join(ref_dir, "GPPComplex.cu")
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.isfile(src) or not os.path.exists(nvcc):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    target = os.path.join(REF_OUT, "GPPComplex.cubin")
+    if force or _stale(target, [src, os.path.join(ref_dir, "GPPComplex.h")]):
+        # The reference's own device flags (Makefile.cuda:9-10), with its
+        # sm_30 target replaced by sm_103a.
+        _run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+              "--maxrregcount=150", "-w", "-I", ref_dir, src, "-o", target + ".tmp"])
+        os.replace(target + ".tmp", target)
     return True
 
 
