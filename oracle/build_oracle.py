@@ -12,10 +12,13 @@ Two products:
     - ``libref_kerseq.so``:      gppKerSeq.cpp      + ref_harness.cpp
     - ``gppKerSeq.ex``, ``gppComplex_seq.ex``, ``gppOpenMP3.ex``: the
       unmodified reference executables (README known-answer runs, CPU timing).
-    - ``GPPComplex.cubin``: the device code of the reference's own CUDA
-      version (GPPComplex.cu) for sm_103a, loaded by oracle/ref_gpu.py to
-      time the reference's GPU kernels beside the new ones.  Device code has
-      no host architecture, so it runs on the GPU host as built here.
+    - ``GPPComplex.cubin`` and ``gppCuda.cubin``: the device code of the
+      reference's two CUDA versions (GPPComplex.cu, called by gppCudaVer.cpp;
+      gppCuda.cu, the unified-memory one) for sm_103a, loaded by
+      oracle/ref_gpu.py to time the reference's GPU kernels beside the new
+      ones.  Device code has no host architecture, so it runs on the GPU host
+      as built here.  gppCuda.cu compiles with cuda13_prefetch_shim.h
+      force-included (an overload of the pre-CUDA-13 cudaMemPrefetchAsync).
   The reference's main() is renamed with -Dmain=... in the library builds.
 """
 from __future__ import annotations
@@ -88,20 +91,26 @@ def build_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool
 
 
 def build_reference_cubin(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool:
-    """Compile GPPComplex.cu's kernels (device code only) into
-    oracle/_ref/GPPComplex.cubin; False without the sources or nvcc."""
-    src = os.path.join(ref_dir, "GPPComplex.cu")
+    """Compile the reference's CUDA kernels (device code only) into
+    oracle/_ref/{GPPComplex,gppCuda}.cubin; False without the sources or nvcc."""
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not os.path.isfile(src) or not os.path.exists(nvcc):
+    if not os.path.isfile(os.path.join(ref_dir, "GPPComplex.cu")) or not os.path.exists(nvcc):
         return False
     os.makedirs(REF_OUT, exist_ok=True)
-    target = os.path.join(REF_OUT, "GPPComplex.cubin")
-    if force or _stale(target, [src, os.path.join(ref_dir, "GPPComplex.h")]):
-        # The reference's own device flags (Makefile.cuda:9-10), with its
-        # sm_30 target replaced by sm_103a.
-        _run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-              "--maxrregcount=150", "-w", "-I", ref_dir, src, "-o", target + ".tmp"])
-        os.replace(target + ".tmp", target)
+    shim = os.path.join(HERE, "cuda13_prefetch_shim.h")
+    # GPPComplex.cu with the reference's own device flags (Makefile.cuda:9-10),
+    # its sm_30 target replaced by sm_103a; gppCuda.cu has no build line in
+    # the reference, so plain -O3.
+    jobs = [("GPPComplex.cubin", "GPPComplex.cu", ["--maxrregcount=150"],
+             [os.path.join(ref_dir, "GPPComplex.h")]),
+            ("gppCuda.cubin", "gppCuda.cu", ["-include", shim], [shim])]
+    for out, src, extra, deps in jobs:
+        srcp = os.path.join(ref_dir, src)
+        target = os.path.join(REF_OUT, out)
+        if force or _stale(target, [srcp] + deps):
+            _run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-w",
+                  "-I", ref_dir] + extra + [srcp, "-o", target + ".tmp"])
+            os.replace(target + ".tmp", target)
     return True
 
 
