@@ -27,7 +27,7 @@ def shapes(n=48, seed=2026):
         nb = int(rng.integers(1, 33 if nw <= 9 else 12))
         nv = int(rng.integers(0, nb + 1))
         nc = int(rng.integers(1, 2500))
-        ng = int(rng.integers(1, 40 if nw <= 9 else 12))
+        ng = min(int(rng.integers(1, 40 if nw <= 9 else 12)), nc)  # ng distinct columns
         near = float(rng.choice([0.0, 0.05]))
         over = int(rng.integers(0, 3)) if ng > 3 else 0
         sem = "kerseq" if i % 3 == 2 else "complex_seq"
