@@ -27,7 +27,7 @@ DRIVER = os.path.join(LIBDIR, "gpp_driver.ex")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["gpp_api.cu", "gpp_fp64.cu", "gpp_mixed.cu", "gpp_batched.cu", "gpp_static.cu",
-               "gpp_compat.cpp"]
+               "gpp_gemm.cu", "gpp_compat.cpp"]
 DRIVER_SOURCES = ["gpp_driver.cpp"]
 
 
@@ -78,7 +78,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 f.result()
     lib_objs = [os.path.join(OBJDIR, n + ".o") for n in LIB_SOURCES]
     if force or _stale(LIB, lib_objs):
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *lib_objs]
+        # cuBLAS (the band-independent FP64 path's ZGEMM) from the toolkit
+        # that compiles the library, found at run time through the rpath.
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(_nvcc()))), "lib64")
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *lib_objs, "-lcublas",
+               "-Xlinker", f"-rpath,{cudalib}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -72,6 +72,7 @@ _SIGS = {
     "gpp_selftest_wait_timeout": (_i, [_i, _vp]),
     "gpp_set_dropin_precision": (_i, [_i]),
     "gpp_get_dropin_precision": (_i, []),
+    "gpp_set_gemm_path": (_i, [_i]),
 }
 
 _lib = None

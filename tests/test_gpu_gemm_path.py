@@ -1,0 +1,102 @@
+"""The band-sum GEMM path of FP64 calls with band-independent frequencies:
+the same sums as the per-term kernel and the oracle (achtemp, asxtemp,
+acht_n1_loc, the static term), on ragged shapes, clamped G' indices,
+near-pole wtilde, every frequency-chunk width and the overlapped host path."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from gppsigma import build, capi, workload as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FP64_TOL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    build.build()
+    capi.load()
+
+
+def band_independent(shape, seed):
+    inp = W.make_inputs(shape, seed)
+    inp.wx_array = inp.wx_array[:1].copy()  # one wx row for every band
+    return inp
+
+
+def sigma_with(mode, d, semantics, n1):
+    from gppsigma import ops
+    lib = capi.load()
+    capi.check(lib.gpp_set_gemm_path(mode), "gemm path")
+    try:
+        r = ops.sigma(d, "fp64", semantics, acht_n1=n1, achstemp=True)
+        ops.wait()
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
+    return r
+
+
+@pytest.mark.parametrize("shape,semantics", [
+    (W.Shape(40, 2, 777, 13, 3, near_pole=0.05), "complex_seq"),
+    (W.Shape(37, 0, 1000, 21, 1), "complex_seq"),
+    (W.Shape(33, 5, 640, 8, 5, igp_overflow=2), "kerseq"),
+    (W.Shape(64, 3, 2048, 64, 8, dw=0.25), "complex_seq"),
+    (W.Shape(20, 4, 300, 1, 3), "kerseq"),
+])
+def test_gemm_path_equals_per_term_kernel_and_oracle(shape, semantics):
+    import oracle_py
+    from gppsigma import ops
+    inp = band_independent(shape, 91)
+    want = oracle_py.run(inp, semantics)
+    d = ops.DeviceInputs.from_host(inp)
+    assert d.wx_stride == 0
+    n1 = shape.nw >= 3
+    g = sigma_with(1, d, semantics, n1)
+    t = sigma_with(0, d, semantics, n1)
+    for key in ("achtemp", "asxtemp", "achstemp"):
+        a, b = getattr(g, key).cpu().numpy(), getattr(t, key).cpu().numpy()
+        assert rel_err(a, want[key]) <= FP64_TOL, key
+        assert rel_err(a, b) <= FP64_TOL, key
+    if n1:
+        a = g.acht_n1_loc.cpu().numpy()
+        scale = np.max(np.abs(want["acht_n1_loc"]))
+        assert np.max(np.abs(a - want["acht_n1_loc"])) <= FP64_TOL * scale
+        assert np.max(np.abs(a - t.acht_n1_loc.cpu().numpy())) <= FP64_TOL * scale
+
+
+def test_gemm_path_is_bit_reproducible_and_automatic_from_32_bands():
+    from gppsigma import ops
+    d = ops.DeviceInputs.from_host(band_independent(W.Shape(64, 2, 1500, 30, 3), 5))
+    a = sigma_with(-1, d, "complex_seq", True)
+    b = sigma_with(-1, d, "complex_seq", True)
+    g = sigma_with(1, d, "complex_seq", True)
+    for key in ("achtemp", "acht_n1_loc"):
+        x, y, z = (getattr(r, key).cpu().numpy() for r in (a, b, g))
+        assert np.array_equal(x, y) and np.array_equal(x, z), key
+    lib = capi.load()
+    assert lib.gpp_set_gemm_path(2) == capi.GPP_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("ngpown", [33, 4])
+def test_gemm_path_through_the_host_pieces(ngpown):
+    """gpp_sigma_host splits the G' rows into pieces; the GEMM path runs per
+    piece and must give the device call's bits."""
+    from gppsigma import ops
+    inp = band_independent(W.Shape(48, 2, 900, ngpown, 3), 17)
+    d = ops.DeviceInputs.from_host(inp)
+    dev = sigma_with(1, d, "complex_seq", True)
+    arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
+                                           "vcoul", "inv_igp_index", "indinv", "wx_array")}
+    lib = capi.load()
+    capi.check(lib.gpp_set_gemm_path(1), "gemm path")
+    try:
+        with ops.HostContext() as ctx:
+            host = ctx.sigma(arrays, inp.shape, "fp64", acht_n1=True)
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
+    assert np.array_equal(host["achtemp"], dev.achtemp.cpu().numpy())
+    assert np.array_equal(host["acht_n1_loc"], dev.acht_n1_loc.cpu().numpy())
