@@ -367,7 +367,10 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
             part.ach_tile0 = (int)tiles_f;
             if (k == 0 && t_timing && t_ev0) cudaEventRecord(t_ev0, s);
             if (gemm) {
-                st = launch_noflag_gemm(p, part, w + o_gemm, nb0, nb1, s, rt);
+                st = GPP_OK;
+                if (k == 0) st = gemm_band_sum(p, part, w + o_gemm, nb0, nb1, s);
+                if (st == GPP_OK) st = gemm_rows(p, part, w + o_gemm, nb0, nb1, s, rt);
+                if (st == GPP_OK && k == pc.n - 1) st = gemm_per_band(p, part, w + o_gemm, nb0, nb1, s);
                 if (st != GPP_OK) {
                     cudaFreeAsync(ws, s);
                     return st;

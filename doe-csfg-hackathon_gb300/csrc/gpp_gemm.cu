@@ -211,68 +211,96 @@ size_t gemm_bytes(const Problem &p, int bands, bool want_n1) {
     return b;
 }
 
-gpp_status launch_noflag_gemm(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                              cudaStream_t s, RowTiles rows) {
-    const int row_tiles = ceil_div(p.ng, 2);
-    const RowTiles rt = rows.clip(row_tiles);
-    if (rt.end <= rt.begin || b1 <= b0) return GPP_OK;
-    const int K = b1 - b0;
-    const int r0 = 2 * rt.begin, r1 = std::min(2 * rt.end, p.ng), nr = r1 - r0;
+namespace {
+
+struct GemmBuffers {
+    double2 *C, *G, *M2, *H;
+};
+
+GemmBuffers carve(const Problem &p, void *ws, int K, bool want_n1) {
     const size_t ng = (size_t)p.ng, nc = (size_t)p.nc;
     char *w = static_cast<char *>(ws);
-    double2 *C = reinterpret_cast<double2 *>(w);
+    GemmBuffers b{};
+    b.C = reinterpret_cast<double2 *>(w);
     w += align_up(sizeof(double2) * (size_t)K * ng);
-    double2 *G = reinterpret_cast<double2 *>(w);
+    b.G = reinterpret_cast<double2 *>(w);
     w += align_up(sizeof(double2) * ng * nc);
-    const bool want_n1 = part.n1 != nullptr;
-    double2 *M2 = want_n1 ? reinterpret_cast<double2 *>(w) : nullptr;
-    if (want_n1) w += align_up(sizeof(double2) * ng * nc);
-    double2 *H = want_n1 ? reinterpret_cast<double2 *>(w) : nullptr;
+    if (want_n1) {
+        b.M2 = reinterpret_cast<double2 *>(w);
+        w += align_up(sizeof(double2) * ng * nc);
+        b.H = reinterpret_cast<double2 *>(w);
+    }
+    return b;
+}
 
-    gemm_coeff_kernel<<<grid_for((long long)K * nr), kThreads, 0, s>>>(p, b0, K, r0, r1, C,
-                                                                       part.err);
+const cuDoubleComplex kOne = {1.0, 0.0}, kZero = {0.0, 0.0};
+
+}  // namespace
+
+gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                         cudaStream_t s) {
+    const int K = b1 - b0;
+    if (K <= 0 || p.ng <= 0) return GPP_OK;
+    const GemmBuffers b = carve(p, ws, K, part.n1 != nullptr);
+    gemm_coeff_kernel<<<grid_for((long long)K * p.ng), kThreads, 0, s>>>(p, b0, K, 0, p.ng, b.C,
+                                                                         part.err);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_coeff_kernel");
-
     cublasHandle_t h = nullptr;
     cublasStatus_t bs = blas_handle(s, &h);
     if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasCreate/cublasSetStream");
-    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-    const cuDoubleComplex *aq = reinterpret_cast<const cuDoubleComplex *>(p.aqsn + (size_t)b0 * nc);
     // Column-major view: aqsn rows are columns of an (nc x K) matrix, C of an
     // (ng x K) one, G of an (nc x ng) one: G = aqsn * C^T.
-    bs = cublasZgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, p.nc, nr, K, &one, aq, p.nc,
-                     reinterpret_cast<const cuDoubleComplex *>(C + r0), p.ng, &zero,
-                     reinterpret_cast<cuDoubleComplex *>(G + (size_t)r0 * nc), p.nc);
+    bs = cublasZgemm(h, CUBLAS_OP_N, CUBLAS_OP_T, p.nc, p.ng, K, &kOne,
+                     reinterpret_cast<const cuDoubleComplex *>(p.aqsn + (size_t)b0 * p.nc), p.nc,
+                     reinterpret_cast<const cuDoubleComplex *>(b.C), p.ng, &kZero,
+                     reinterpret_cast<cuDoubleComplex *>(b.G), p.nc);
     if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasZgemm (band sum)");
+    return GPP_OK;
+}
 
+gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                     cudaStream_t s, RowTiles rows) {
+    const RowTiles rt = rows.clip(ceil_div(p.ng, 2));
+    if (rt.end <= rt.begin || b1 <= b0) return GPP_OK;
+    const GemmBuffers b = carve(p, ws, b1 - b0, part.n1 != nullptr);
+    cudaError_t e;
     switch (nwc_of(p.nw)) {
-        case 1: e = launch_epilogue_t<1>(p, part, G, rt, s); break;
-        case 2: e = launch_epilogue_t<2>(p, part, G, rt, s); break;
-        case 3: e = launch_epilogue_t<3>(p, part, G, rt, s); break;
-        case 4: e = launch_epilogue_t<4>(p, part, G, rt, s); break;
-        default: e = launch_epilogue_t<8>(p, part, G, rt, s); break;
+        case 1: e = launch_epilogue_t<1>(p, part, b.G, rt, s); break;
+        case 2: e = launch_epilogue_t<2>(p, part, b.G, rt, s); break;
+        case 3: e = launch_epilogue_t<3>(p, part, b.G, rt, s); break;
+        case 4: e = launch_epilogue_t<4>(p, part, b.G, rt, s); break;
+        default: e = launch_epilogue_t<8>(p, part, b.G, rt, s); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "gemm_epilogue_kernel");
+    return GPP_OK;
+}
 
-    if (want_n1) {
-        gemm_m2_kernel<<<grid_for((long long)nr * p.nc), kThreads, 0, s>>>(p, r0, r1, M2);
-        count_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
-        // H (column-major ng x K) = M_2^T * aqsn, rows [r0, r1).
-        bs = cublasZgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, nr, K, p.nc, &one,
-                         reinterpret_cast<const cuDoubleComplex *>(M2 + (size_t)r0 * nc), p.nc,
-                         aq, p.nc, &zero, reinterpret_cast<cuDoubleComplex *>(H + r0), p.ng);
-        if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasZgemm (per-band output)");
-        const int tiles = rt.end - rt.begin;
-        gemm_n1_kernel<<<grid_for((long long)K * tiles), kThreads, 0, s>>>(p, part, b0, K, rt.begin,
-                                                                           tiles, C, H);
-        count_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return cuda_fail(e, "gemm_n1_kernel");
-    }
+gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                         cudaStream_t s) {
+    const int K = b1 - b0;
+    if (K <= 0 || p.ng <= 0 || !part.n1) return GPP_OK;
+    const GemmBuffers b = carve(p, ws, K, true);
+    gemm_m2_kernel<<<grid_for((long long)p.ng * p.nc), kThreads, 0, s>>>(p, 0, p.ng, b.M2);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
+    cublasHandle_t h = nullptr;
+    cublasStatus_t bs = blas_handle(s, &h);
+    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasCreate/cublasSetStream");
+    // H (column-major ng x K) = M_2^T * aqsn.
+    bs = cublasZgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, p.ng, K, p.nc, &kOne,
+                     reinterpret_cast<const cuDoubleComplex *>(b.M2), p.nc,
+                     reinterpret_cast<const cuDoubleComplex *>(p.aqsn + (size_t)b0 * p.nc), p.nc,
+                     &kZero, reinterpret_cast<cuDoubleComplex *>(b.H), p.ng);
+    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasZgemm (per-band output)");
+    const int tiles = ceil_div(p.ng, 2);
+    gemm_n1_kernel<<<grid_for((long long)K * tiles), kThreads, 0, s>>>(p, part, b0, K, 0, tiles,
+                                                                       b.C, b.H);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "gemm_n1_kernel");
     return GPP_OK;
 }
 

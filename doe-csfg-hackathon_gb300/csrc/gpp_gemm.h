@@ -9,13 +9,23 @@
 
 namespace gpp {
 
-// Workspace bytes of launch_noflag_gemm for `bands` unoccupied bands.
+// Workspace bytes of the GEMM path for `bands` unoccupied bands.
 size_t gemm_bytes(const Problem &p, int bands, bool want_n1);
 
-// Unoccupied bands [b0, b1) of a problem with wx_stride == 0: one achtemp
-// partial per row tile (slot part.ach_tile0 + row tile) and, when part.n1 is
-// set, per-band partials (nw >= 3).  `ws` holds gemm_bytes(p, b1 - b0, ...).
-gpp_status launch_noflag_gemm(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                              cudaStream_t s, RowTiles rows = RowTiles());
+// Unoccupied bands [b0, b1) of a problem with wx_stride == 0, in three
+// steps on stream s, each over every G' row so that the results do not
+// depend on how a caller splits the rows:
+//  1. gemm_band_sum: c and G = sum_n1 c aqsn (needs the band arrays only);
+//  2. gemm_rows: for row tiles `rows`, the achtemp partial of each row tile
+//     (slot part.ach_tile0 + row tile) -- needs those rows' wtilde/I_eps;
+//  3. gemm_per_band: when part.n1 is set (nw >= 3), the per-band partials
+//     of acht_n1_loc -- needs every row.
+// `ws` holds gemm_bytes(p, b1 - b0, part.n1 != nullptr).
+gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                         cudaStream_t s);
+gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                     cudaStream_t s, RowTiles rows = RowTiles());
+gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b0, int b1,
+                         cudaStream_t s);
 
 }  // namespace gpp
