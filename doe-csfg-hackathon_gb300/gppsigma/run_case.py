@@ -30,6 +30,8 @@ def main() -> int:
     ap.add_argument("--semantics", default="complex_seq", choices=["complex_seq", "kerseq"])
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--seed", type=int, default=20240607)
+    ap.add_argument("--band-independent", action="store_true",
+                    help="one wx row for every band (the reference's wx_array[3])")
     args = ap.parse_args()
 
     import torch
@@ -38,6 +40,10 @@ def main() -> int:
     torch.cuda.set_device(0)
     shape = SHAPES[args.workload]
     d = ops.device_inputs(shape, args.seed)
+    if args.band_independent:
+        import dataclasses
+        d = dataclasses.replace(d, wx_array=d.wx_array.reshape(-1, shape.nw)[:1].contiguous(),
+                                wx_stride=0)
     out = None
     for i in range(args.repeat):
         t0 = time.perf_counter()
