@@ -14,6 +14,7 @@
 
 #include "gpp_gb300.h"
 #include "gpp_gemm.h"
+#include "gpp_gemm_mixed.h"
 #include "gpp_kernels.h"
 
 namespace gpp {
@@ -220,13 +221,16 @@ int dropin_precision() {
     return env;
 }
 
-// Whether the unoccupied bands of an FP64 call with band-independent wx go
-// through the band-sum GEMM (gpp_gemm.cu): automatically from 32 unoccupied
-// bands on (below that the per-term kernel is as fast), or as
-// gpp_set_gemm_path forces.
+// Whether the unoccupied bands of a call with band-independent wx go through
+// the band-sum GEMM (FP64: gpp_gemm.cu, mixed: gpp_gemm_mixed.cu):
+// automatically from 32 unoccupied bands on (below that the per-term kernel
+// is as fast), or as gpp_set_gemm_path forces.
 constexpr int kGemmMinBands = 32;
-bool gemm_path(int precision, int wx_stride, int bands) {
-    if (precision != GPP_PRECISION_FP64 || wx_stride != 0 || bands <= 0) return false;
+// Mixed-precision calls take it only without the per-band output (which
+// would need a second band-sum product; the per-term kernel produces it).
+bool gemm_path(int precision, int wx_stride, int bands, bool want_n1) {
+    if (wx_stride != 0 || bands <= 0) return false;
+    if (precision == GPP_PRECISION_MIXED && want_n1) return false;
     return t_gemm_path < 0 ? bands >= kGemmMinBands : t_gemm_path == 1;
 }
 
@@ -288,7 +292,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
 
     const TileShape fs = flag_shape(p);  // same tiling for the FP64 and the mixed occupied tile
     const TileShape ns = mixed ? mixed_noflag_shape(p) : fp64_noflag_shape(p);
-    const bool gemm = has_noflag && gemm_path(precision, p.wx_stride, nb1 - nb0);
+    const bool want_n1 = o.n1 && p.nw >= 3 && p.ng > 0;
+    const bool gemm = has_noflag && gemm_path(precision, p.wx_stride, nb1 - nb0, want_n1);
     const long long rows_f = has_flag ? ceil_div(p.ng, fs.rg) : 0;
     const long long rows_n = has_noflag ? ceil_div(p.ng, ns.rg) : 0;
     const long long tiles_f = has_flag ? rows_f * (fb1 - fb0) : 0;
@@ -303,7 +308,6 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         return fail(GPP_ERR_UNSUPPORTED, "occupied-band launches start at band 0");
     const long long ach_seg = tiles_f + tiles_n;
     const long long n1_seg = rows_f > rows_n ? rows_f : rows_n;
-    const bool want_n1 = o.n1 && p.nw >= 3 && p.ng > 0;
     const bool want_achs = (o.achs || o.achs_re) && p.ng > 0 && b1 > b0;
     const int achs_blocks = want_achs ? achstemp_blocks(p) : 0;
 
@@ -313,7 +317,9 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const size_t o_n1 = off; off = align_up(off + (want_n1 ? sizeof(double2) * (size_t)(n1_seg * p.nb) : 0));
     const size_t o_st = off; off = align_up(off + sizeof(double2) * (size_t)achs_blocks);
     const size_t o_split = off; off = align_up(off + (mixed ? mixed_split_bytes(p) : 0));
-    const size_t o_gemm = off; off = align_up(off + (gemm ? gemm_bytes(p, nb1 - nb0, want_n1) : 0));
+    const size_t gemm_ws = !gemm ? 0 : mixed ? mixed_gemm_bytes(p, nb1 - nb0)
+                                            : gemm_bytes(p, nb1 - nb0, want_n1);
+    const size_t o_gemm = off; off = align_up(off + gemm_ws);
     const size_t ws_bytes = off > 0 ? off : 256;
 
     void *ws = nullptr;
@@ -366,7 +372,16 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         if (e == cudaSuccess && has_noflag) {
             part.ach_tile0 = (int)tiles_f;
             if (k == 0 && t_timing && t_ev0) cudaEventRecord(t_ev0, s);
-            if (gemm) {
+            if (gemm && mixed) {
+                st = GPP_OK;
+                if (k == 0) st = mixed_gemm_band_sum(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
+                if (st == GPP_OK)
+                    st = mixed_gemm_rows(p, part, w + o_split, w + o_gemm, nb0, nb1, s, rt);
+                if (st != GPP_OK) {
+                    cudaFreeAsync(ws, s);
+                    return st;
+                }
+            } else if (gemm) {
                 st = GPP_OK;
                 if (k == 0) st = gemm_band_sum(p, part, w + o_gemm, nb0, nb1, s);
                 if (st == GPP_OK) st = gemm_rows(p, part, w + o_gemm, nb0, nb1, s, rt);

@@ -1,0 +1,284 @@
+// gpp_gemm_mixed.cu -- unoccupied bands with band-independent frequencies in
+// mixed precision: the band sum G = sum_n1 c aqsn as a float-float complex
+// GEMM on the FP32 pipes, then the frequency pass on G (the FP64 form of the
+// same factorisation, and its derivation, is gpp_gemm.cu).
+//
+// The GEMM keeps the packed layout of the mixed kernels: a thread owns one
+// G' row pair -- the two lanes of every f32x2 instruction -- and 8 columns,
+// so one complex float-float multiply-add of both rows is 48 packed
+// instructions (4 products, 4 TwoSum-based additions).  A block computes 16
+// row pairs x 128 columns, staging 16 bands of c and aqsn per step in shared
+// memory.  G is written as row-pair planes like wtilde and Q, and the
+// frequency pass reads it exactly as the per-term kernel reads aqsn * Q:
+// terms within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs
+// and G.  Compared with the per-term kernel the division runs once per
+// (row, column, frequency) instead of once per band.
+#include "gpp_gemm_mixed.h"
+#include "gpp_tiles_mixed.cuh"
+
+namespace gpp {
+
+gpp_status set_error(gpp_status s, const char *msg);
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kPairs = 16;   // row pairs per GEMM block
+constexpr int kCols = 128;   // columns per GEMM block
+constexpr int kStep = 16;    // bands per shared-memory step
+constexpr int kPerThread = kCols / (kThreads / kPairs);  // columns per thread (8)
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+int row_pairs(const Problem &p) { return (p.ng + 1) / 2; }
+
+gpp_status cuda_fail(cudaError_t e, const char *what) {
+    char buf[256];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return set_error(e == cudaErrorMemoryAllocation ? GPP_ERR_OUT_OF_MEMORY : GPP_ERR_CUDA, buf);
+}
+
+// c[k][j] = 0.5 vcoul[igp] conj(aqsm[b0 + k][igp]) for rows 2j, 2j+1 as
+// float-float lanes: two float4 (re, im), each (hi r0, hi r1, lo r0, lo r1).
+// A row past ngpown or with an invalid G' index contributes 0.
+__global__ void __launch_bounds__(kThreads) mg_coeff_kernel(Problem p, int b0, int K,
+                                                            float4 *cpl, int *err) {
+    const int pairs = (p.ng + 1) / 2;
+    const long long n = (long long)K * pairs;
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        const int k = (int)(i / pairs), j = (int)(i % pairs);
+        df re[2], im[2];
+        for (int g = 0; g < 2; ++g) {
+            const int r = 2 * j + g;
+            double2 c = make_double2(0.0, 0.0);
+            if (r < p.ng) {
+                const int igp = resolve_igp(p, r, err);
+                if (igp >= 0) {
+                    const double2 m = __ldg(p.aqsm + (size_t)(b0 + k) * p.nc + igp);
+                    c = cscale(make_double2(0.5 * m.x, -0.5 * m.y), __ldg(p.vcoul + igp));
+                }
+            }
+            re[g] = split_bits(c.x);
+            im[g] = split_bits(c.y);
+        }
+        cpl[i * 2] = make_float4(re[0].h, re[1].h, re[0].l, re[1].l);
+        cpl[i * 2 + 1] = make_float4(im[0].h, im[1].h, im[0].l, im[1].l);
+    }
+}
+
+// G[j][col] = sum_k c[k][j] aqsn[k][col] in float-float, both rows of pair j
+// as the lanes.  Grid: x over blocks of kPairs row pairs (fastest, so blocks
+// in flight share their aqsn columns in L2), y over blocks of kCols columns.
+__global__ void __launch_bounds__(kThreads, 2) mg_gemm_kernel(int K, int pairs, int nc,
+                                                              const float4 *__restrict__ cpl,
+                                                              const float4 *__restrict__ band,
+                                                              float4 *__restrict__ G) {
+    __shared__ float4 sA[kStep][kPairs][2];
+    __shared__ float4 sB[kStep][kCols];
+    const int tid = threadIdx.x;
+    const int pr = tid / (kThreads / kPairs), cg = tid % (kThreads / kPairs);
+    const int pair0 = blockIdx.x * kPairs, col0 = blockIdx.y * kCols;
+    const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    df2 accr[kPerThread], acci[kPerThread];
+#pragma unroll
+    for (int t = 0; t < kPerThread; ++t) accr[t] = acci[t] = z;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k0 = 0; k0 < K; k0 += kStep) {
+        const int kc = min(kStep, K - k0);
+        __syncthreads();  // the previous step's operands are consumed
+        for (int i = tid; i < kStep * kPairs * 2; i += kThreads) {
+            const int kk = i / (kPairs * 2), pp = (i / 2) % kPairs, c = i % 2;
+            float4 v = zero4;
+            if (kk < kc && pair0 + pp < pairs)
+                v = cpl[((size_t)(k0 + kk) * pairs + pair0 + pp) * 2 + c];
+            sA[kk][pp][c] = v;
+        }
+        for (int i = tid; i < kStep * kCols; i += kThreads) {
+            const int kk = i / kCols, cc = i % kCols;
+            float4 v = zero4;
+            if (kk < kc && col0 + cc < nc) v = band[(size_t)(k0 + kk) * nc + col0 + cc];
+            sB[kk][cc] = v;
+        }
+        __syncthreads();
+        for (int kk = 0; kk < kc; ++kk) {
+            const float4 a4 = sA[kk][pr][0], b4 = sA[kk][pr][1];
+            const df2 ar = {f2(a4.x, a4.y), f2(a4.z, a4.w)};
+            const df2 ai = {f2(b4.x, b4.y), f2(b4.z, b4.w)};
+#pragma unroll
+            for (int t = 0; t < kPerThread; ++t) {
+                const float4 v = sB[kk][cg + t * (kThreads / kPairs)];
+                const df2 br = df2_bcast(df{v.x, v.y}), bi = df2_bcast(df{v.z, v.w});
+                accr[t] = df2_sub(df2_add(accr[t], df2_mul(ar, br)), df2_mul(ai, bi));
+                acci[t] = df2_add(df2_add(acci[t], df2_mul(ar, bi)), df2_mul(ai, br));
+            }
+        }
+    }
+    const int j = pair0 + pr;
+    if (j >= pairs) return;
+#pragma unroll
+    for (int t = 0; t < kPerThread; ++t) {
+        const int col = col0 + cg + t * (kThreads / kPairs);
+        if (col >= nc) continue;
+        G[(size_t)j * 2 * nc + col] = make_float4(accr[t].h.x, accr[t].h.y, accr[t].l.x, accr[t].l.y);
+        G[(size_t)j * 2 * nc + nc + col] =
+            make_float4(acci[t].h.x, acci[t].h.y, acci[t].l.x, acci[t].l.y);
+    }
+}
+
+// A G term near the pole in FP64: G from its float-float value, wtilde and
+// I_eps from the inputs.  Out of line, returning whole pairs.
+static __device__ __noinline__ TermPair mg_pole_pair(const Problem &p, df2 d, float thr, int row0,
+                                                     int ig, int iw, df2 Gr, df2 Gi, TermPair t) {
+    const double wx = __ldg(p.wx + iw);
+    for (int g = 0; g < 2; ++g) {
+        if ((g == 0 ? d.h.x : d.h.y) >= thr) continue;
+        const int row = min(row0 + g, p.ng - 1);
+        const double2 wt = __ldg(p.wt + (size_t)row * p.nc + ig);
+        const double2 ie = __ldg(p.ieps + (size_t)row * p.nc + ig);
+        const double2 Gv = make_double2(to_double(df2_lane(Gr, g)), to_double(df2_lane(Gi, g)));
+        const double2 A = cmul(Gv, cmul(wt, ie));
+        const double wr = wx - wt.x;
+        const double r = 1.0 / (wr * wr + wt.y * wt.y);
+        df2_set_lane(t.re, g, split((A.x * wr - A.y * wt.y) * r));
+        df2_set_lane(t.im, g, split((A.y * wr + A.x * wt.y) * r));
+    }
+    return t;
+}
+
+// The frequency pass: one block per row pair, threads over ig; the row
+// tile's sum of G Q conj(wdiff) / |wdiff|^2 per frequency into its partial.
+template <int NWC>
+__global__ void __launch_bounds__(128) mg_freq_kernel(Problem p, Partials part, SplitPlanes s,
+                                                      int wx_band, const float4 *__restrict__ G,
+                                                      int row_tile0) {
+    constexpr int THREADS = 128, K = NWC * 2;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+    const int j = row_tile0 + blockIdx.x;
+    const int iw0 = blockIdx.y * NWC;
+    const int nc = p.nc, row0 = 2 * j;
+    df wx[NWC];
+    float thr[NWC];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w) {
+        const float2 x = s.wx[(size_t)wx_band * p.nw + min(iw0 + w, p.nw - 1)];
+        wx[w] = {x.x, x.y};
+        thr[w] = 1e-6f * x.x * x.x;
+    }
+    const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    df2 acc[NWC][2];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w) acc[w][0] = acc[w][1] = z;
+    const float4 *rp = s.rows + (size_t)j * 4 * nc;
+    const float4 *gp = G + (size_t)j * 2 * nc;
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        const float4 vr = __ldg(rp + ig), vi = __ldg(rp + nc + ig);
+        const float4 vqr = __ldg(rp + 2 * nc + ig), vqi = __ldg(rp + 3 * nc + ig);
+        const float4 g4r = __ldg(gp + ig), g4i = __ldg(gp + nc + ig);
+        const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)}, wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
+        const df2 qr = {f2(vqr.x, vqr.y), f2(vqr.z, vqr.w)};
+        const df2 qi = {f2(vqi.x, vqi.y), f2(vqi.z, vqi.w)};
+        const df2 Gr = {f2(g4r.x, g4r.y), f2(g4r.z, g4r.w)};
+        const df2 Gi = {f2(g4i.x, g4i.y), f2(g4i.z, g4i.w)};
+        const df2 Ar = df2_sub(df2_mul(Gr, qr), df2_mul(Gi, qi));  // A = G Q
+        const df2 Ai = df2_add(df2_mul(Gr, qi), df2_mul(Gi, qr));
+        const df2 wti2 = df2_mul(wti, wti);
+        const df2 Ai_wti = df2_mul(Ai, wti), Ar_wti = df2_mul(Ar, wti);
+#pragma unroll
+        for (int w = 0; w < NWC; ++w) {
+            const df2 wr = df2_norm(df2_sub(df2_bcast(wx[w]), wtr));  // Re(wdiff)
+            const df2 d = df2_add(df2_sqr(wr), wti2);                  // |wdiff|^2
+            const df2 r = df2_rcp(d);
+            TermPair t;
+            t.re = df2_mul(df2_sub(df2_mul(Ar, wr), Ai_wti), r);
+            t.im = df2_mul(df2_add(df2_mul(Ai, wr), Ar_wti), r);
+            if (!(d.h.x >= thr[w]) || !(d.h.y >= thr[w]))
+                t = mg_pole_pair(p, d, thr[w], row0, ig, min(iw0 + w, p.nw - 1), Gr, Gi, t);
+            acc[w][0] = df2_add(acc[w][0], t.re);
+            acc[w][1] = df2_add(acc[w][1], t.im);
+        }
+    }
+    // Lanes are the pair's rows; a row past ngpown has G = 0 (c = 0).
+    double v[K];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w)
+#pragma unroll
+        for (int ri = 0; ri < 2; ++ri)
+            v[w * 2 + ri] = to_double(df2_lane(acc[w][ri], 0)) + to_double(df2_lane(acc[w][ri], 1));
+    block_reduce<K, THREADS>(v, red, S);
+    const int w = threadIdx.x;
+    if (w < NWC && iw0 + w < p.nw)
+        part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + j] =
+            make_double2(S[w * 2], S[w * 2 + 1]);
+}
+
+int grid_for(long long n) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want = (n + kThreads - 1) / kThreads;
+    const long long cap = (long long)(sms > 0 ? sms : 132) * 8;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+template <int NWC>
+cudaError_t launch_freq_t(const Problem &p, const Partials &part, const SplitPlanes &s, int wx_band,
+                          const float4 *G, RowTiles r, cudaStream_t st) {
+    dim3 grid((unsigned)(r.end - r.begin), (unsigned)ceil_div(p.nw, NWC));
+    mg_freq_kernel<NWC><<<grid, 128, 0, st>>>(p, part, s, wx_band, G, r.begin);
+    count_launch();
+    return cudaGetLastError();
+}
+
+float4 *planes_c(void *ws) { return static_cast<float4 *>(ws); }
+float4 *planes_g(const Problem &p, void *ws, int K) {
+    return reinterpret_cast<float4 *>(static_cast<char *>(ws) +
+                                      align_up(sizeof(float4) * 2 * (size_t)K * row_pairs(p)));
+}
+
+}  // namespace
+
+size_t mixed_gemm_bytes(const Problem &p, int bands) {
+    return align_up(sizeof(float4) * 2 * (size_t)bands * row_pairs(p)) +
+           align_up(sizeof(float4) * 2 * (size_t)row_pairs(p) * p.nc);
+}
+
+gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *split_ws, void *ws,
+                               int b0, int b1, cudaStream_t st) {
+    const SplitPlanes s = split_planes_at(p, split_ws);
+    const int K = b1 - b0, pairs = row_pairs(p);
+    if (K <= 0 || pairs <= 0) return GPP_OK;
+    float4 *cpl = planes_c(ws);
+    mg_coeff_kernel<<<grid_for((long long)K * pairs), kThreads, 0, st>>>(p, b0, K, cpl, part.err);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_coeff_kernel");
+    dim3 grid((unsigned)ceil_div(pairs, kPairs), (unsigned)ceil_div(p.nc, kCols));
+    mg_gemm_kernel<<<grid, kThreads, 0, st>>>(K, pairs, p.nc, cpl, s.band + (size_t)b0 * p.nc,
+                                              planes_g(p, ws, K));
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_gemm_kernel");
+    return GPP_OK;
+}
+
+gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_ws, void *ws, int b0,
+                           int b1, cudaStream_t st, RowTiles rows) {
+    const SplitPlanes s = split_planes_at(p, split_ws);
+    const RowTiles rt = rows.clip(row_pairs(p));
+    if (rt.end <= rt.begin || b1 <= b0) return GPP_OK;
+    const float4 *G = planes_g(p, ws, b1 - b0);
+    const int nwc = p.nw <= 4 ? p.nw : 8;
+    cudaError_t e;
+    switch (nwc) {
+        case 1: e = launch_freq_t<1>(p, part, s, b0, G, rt, st); break;
+        case 2: e = launch_freq_t<2>(p, part, s, b0, G, rt, st); break;
+        case 3: e = launch_freq_t<3>(p, part, s, b0, G, rt, st); break;
+        case 4: e = launch_freq_t<4>(p, part, s, b0, G, rt, st); break;
+        default: e = launch_freq_t<8>(p, part, s, b0, G, rt, st); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "mg_freq_kernel");
+    return GPP_OK;
+}
+
+}  // namespace gpp

@@ -1,0 +1,30 @@
+// gpp_gemm_mixed.h -- the band-independent-frequency mixed-precision path of
+// the unoccupied bands (gpp_gemm_mixed.cu): the band sum as a float-float
+// complex GEMM.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "gpp_gb300.h"
+#include "gpp_kernels.h"
+
+namespace gpp {
+
+// Workspace bytes for `bands` unoccupied bands.
+size_t mixed_gemm_bytes(const Problem &p, int bands);
+
+// Unoccupied bands [b0, b1) of a problem with wx_stride == 0, achtemp only
+// (no per-band output), on the float-float split planes at `split_ws`
+// (bands and wx split for [b0, b1), rows split before mixed_gemm_rows reads
+// them):
+//  1. mixed_gemm_band_sum: c and G = sum_n1 c aqsn over every G' row;
+//  2. mixed_gemm_rows: for row tiles `rows`, each row tile's achtemp partial
+//     (slot part.ach_tile0 + row tile).
+gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *split_ws, void *ws,
+                               int b0, int b1, cudaStream_t st);
+gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_ws, void *ws, int b0,
+                           int b1, cudaStream_t st, RowTiles rows = RowTiles());
+
+}  // namespace gpp

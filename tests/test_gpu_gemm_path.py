@@ -100,3 +100,57 @@ def test_gemm_path_through_the_host_pieces(ngpown):
         capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
     assert np.array_equal(host["achtemp"], dev.achtemp.cpu().numpy())
     assert np.array_equal(host["acht_n1_loc"], dev.acht_n1_loc.cpu().numpy())
+
+
+MIXED_TOL = 1e-8
+
+
+def mixed_with(mode, d, semantics):
+    from gppsigma import ops
+    lib = capi.load()
+    capi.check(lib.gpp_set_gemm_path(mode), "gemm path")
+    try:
+        r = ops.sigma(d, "mixed", semantics, acht_n1=False, achstemp=False)
+        ops.wait()
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
+    return r
+
+
+@pytest.mark.parametrize("shape,semantics", [
+    (W.Shape(40, 2, 777, 13, 3, near_pole=0.05), "complex_seq"),
+    (W.Shape(37, 0, 1000, 21, 1), "complex_seq"),
+    (W.Shape(33, 5, 640, 8, 5, igp_overflow=2), "kerseq"),
+    (W.Shape(64, 3, 2048, 64, 8, dw=0.25, near_pole=0.02), "complex_seq"),
+    (W.Shape(20, 4, 300, 1, 3), "kerseq"),
+    (W.Shape(150, 2, 4100, 70, 3, near_pole=0.01), "complex_seq"),
+])
+def test_mixed_gemm_path_within_1e8_of_fp64(shape, semantics):
+    """The float-float band-sum GEMM against the FP64 per-term kernel."""
+    from gppsigma import ops
+    d = ops.DeviceInputs.from_host(band_independent(shape, 93))
+    m = mixed_with(1, d, semantics)
+    f = sigma_with(0, d, semantics, False)
+    t = mixed_with(0, d, semantics)
+    for key in ("achtemp", "asxtemp"):
+        a = getattr(m, key).cpu().numpy()
+        assert rel_err(a, getattr(f, key).cpu().numpy()) <= MIXED_TOL, key
+        assert rel_err(a, getattr(t, key).cpu().numpy()) <= MIXED_TOL, key
+
+
+def test_mixed_gemm_path_through_the_host_pieces():
+    from gppsigma import ops
+    inp = band_independent(W.Shape(48, 2, 900, 33, 3, near_pole=0.02), 19)
+    d = ops.DeviceInputs.from_host(inp)
+    dev = mixed_with(1, d, "complex_seq")
+    arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
+                                           "vcoul", "inv_igp_index", "indinv", "wx_array")}
+    lib = capi.load()
+    capi.check(lib.gpp_set_gemm_path(1), "gemm path")
+    try:
+        with ops.HostContext() as ctx:
+            host = ctx.sigma(arrays, inp.shape, "mixed")
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
+    assert np.array_equal(host["achtemp"], dev.achtemp.cpu().numpy())
+    assert np.array_equal(host["asxtemp"], dev.asxtemp.cpu().numpy())
