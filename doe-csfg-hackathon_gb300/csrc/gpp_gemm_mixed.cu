@@ -253,6 +253,8 @@ gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *spl
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "mg_coeff_kernel");
+    if (ceil_div(p.nc, kCols) > 65535)
+        return set_error(GPP_ERR_UNSUPPORTED, "ncouls too large for the band-sum GEMM grid");
     dim3 grid((unsigned)ceil_div(pairs, kPairs), (unsigned)ceil_div(p.nc, kCols));
     mg_gemm_kernel<<<grid, kThreads, 0, st>>>(K, pairs, p.nc, cpl, s.band + (size_t)b0 * p.nc,
                                               planes_g(p, ws, K));
