@@ -132,15 +132,17 @@ gpp_stream_t gpp_get_stream(void);
 gpp_status gpp_set_dropin_precision(int precision);
 int gpp_get_dropin_precision(void);
 
-/* No counterpart in the reference.  How FP64 calls with band-independent
+/* No counterpart in the reference.  How calls with band-independent
  * frequencies (wx_stride == 0: the drop-in entry points and gpp_sigma)
  * compute their unoccupied bands (per host thread): -1 (default) through
  * the band-sum GEMM when there are at least 32 unoccupied bands, 0 always
  * with the per-term kernel, 1 always through the GEMM.  With wx the same
  * for every band the band sum factors out of the division:
- * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM),
- * several times faster in FP64; the results agree with the per-term
- * kernel to FP64 rounding. */
+ * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM:
+ * cuBLAS in FP64, a float-float GEMM on the FP32 pipes in mixed precision),
+ * several times faster; the results agree with the per-term kernels to
+ * their rounding.  Mixed-precision calls that ask for acht_n1_loc keep the
+ * per-term kernel. */
 gpp_status gpp_set_gemm_path(int mode);
 
 /* ------------------------------------------------------------------------
