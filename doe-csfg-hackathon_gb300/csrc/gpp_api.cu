@@ -226,11 +226,10 @@ int dropin_precision() {
 // automatically from 32 unoccupied bands on (below that the per-term kernel
 // is as fast), or as gpp_set_gemm_path forces.
 constexpr int kGemmMinBands = 32;
-// Mixed-precision calls take it only without the per-band output (which
-// would need a second band-sum product; the per-term kernel produces it).
 bool gemm_path(int precision, int wx_stride, int bands, bool want_n1) {
+    (void)precision;
+    (void)want_n1;
     if (wx_stride != 0 || bands <= 0) return false;
-    if (precision == GPP_PRECISION_MIXED && want_n1) return false;
     return t_gemm_path < 0 ? bands >= kGemmMinBands : t_gemm_path == 1;
 }
 
@@ -317,7 +316,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const size_t o_n1 = off; off = align_up(off + (want_n1 ? sizeof(double2) * (size_t)(n1_seg * p.nb) : 0));
     const size_t o_st = off; off = align_up(off + sizeof(double2) * (size_t)achs_blocks);
     const size_t o_split = off; off = align_up(off + (mixed ? mixed_split_bytes(p) : 0));
-    const size_t gemm_ws = !gemm ? 0 : mixed ? mixed_gemm_bytes(p, nb1 - nb0)
+    const size_t gemm_ws = !gemm ? 0 : mixed ? mixed_gemm_bytes(p, nb1 - nb0, want_n1)
                                             : gemm_bytes(p, nb1 - nb0, want_n1);
     const size_t o_gemm = off; off = align_up(off + gemm_ws);
     const size_t ws_bytes = off > 0 ? off : 256;
@@ -377,6 +376,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
                 if (k == 0) st = mixed_gemm_band_sum(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
                 if (st == GPP_OK)
                     st = mixed_gemm_rows(p, part, w + o_split, w + o_gemm, nb0, nb1, s, rt);
+                if (st == GPP_OK && k == pc.n - 1)
+                    st = mixed_gemm_per_band(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
                 if (st != GPP_OK) {
                     cudaFreeAsync(ws, s);
                     return st;

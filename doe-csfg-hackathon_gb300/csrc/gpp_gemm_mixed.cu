@@ -212,6 +212,145 @@ __global__ void __launch_bounds__(128) mg_freq_kernel(Problem p, Partials part, 
             make_double2(S[w * 2], S[w * 2 + 1]);
 }
 
+// M_2[j][ig] = Q conj(wdiff) / |wdiff|^2 at iw = 2 for row pair j, in
+// float-float lanes (FP64 from the inputs within 1e-3 |wx| of the pole),
+// stored as two planes (re, im) per row pair.
+static __device__ __noinline__ TermPair mg_pole_m2(const Problem &p, df2 d, float thr, int row0,
+                                                   int ig, TermPair t) {
+    const double wx = __ldg(p.wx + 2);
+    for (int g = 0; g < 2; ++g) {
+        if ((g == 0 ? d.h.x : d.h.y) >= thr) continue;
+        const int row = min(row0 + g, p.ng - 1);
+        const double2 wt = __ldg(p.wt + (size_t)row * p.nc + ig);
+        const double2 Q = cmul(wt, __ldg(p.ieps + (size_t)row * p.nc + ig));
+        const double wr = wx - wt.x;
+        const double r = 1.0 / (wr * wr + wt.y * wt.y);
+        df2_set_lane(t.re, g, split((Q.x * wr - Q.y * wt.y) * r));
+        df2_set_lane(t.im, g, split((Q.y * wr + Q.x * wt.y) * r));
+    }
+    return t;
+}
+
+__global__ void __launch_bounds__(kThreads) mg_m2_kernel(Problem p, SplitPlanes s, int wx_band,
+                                                         float4 *M2) {
+    const int pairs = (p.ng + 1) / 2;
+    const size_t nc = (size_t)p.nc;
+    const float2 x = s.wx[(size_t)wx_band * p.nw + 2];
+    const df wx = {x.x, x.y};
+    const float thr = 1e-6f * x.x * x.x;
+    const size_t n = (size_t)pairs * nc;
+    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * kThreads) {
+        const size_t j = i / nc, ig = i % nc;
+        const float4 *rp = s.rows + j * 4 * nc;
+        const float4 vr = __ldg(rp + ig), vi = __ldg(rp + nc + ig);
+        const float4 vqr = __ldg(rp + 2 * nc + ig), vqi = __ldg(rp + 3 * nc + ig);
+        const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)}, wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
+        const df2 qr = {f2(vqr.x, vqr.y), f2(vqr.z, vqr.w)};
+        const df2 qi = {f2(vqi.x, vqi.y), f2(vqi.z, vqi.w)};
+        const df2 wr = df2_norm(df2_sub(df2_bcast(wx), wtr));
+        const df2 d = df2_add(df2_sqr(wr), df2_mul(wti, wti));
+        const df2 r = df2_rcp(d);
+        TermPair t;
+        t.re = df2_mul(df2_sub(df2_mul(qr, wr), df2_mul(qi, wti)), r);
+        t.im = df2_mul(df2_add(df2_mul(qi, wr), df2_mul(qr, wti)), r);
+        if (!(d.h.x >= thr) || !(d.h.y >= thr)) t = mg_pole_m2(p, d, thr, (int)(2 * j), (int)ig, t);
+        M2[j * 2 * nc + ig] = make_float4(t.re.h.x, t.re.h.y, t.re.l.x, t.re.l.y);
+        M2[j * 2 * nc + nc + ig] = make_float4(t.im.h.x, t.im.h.y, t.im.l.x, t.im.l.y);
+    }
+}
+
+constexpr int kHBands = 128;   // bands per H block
+constexpr int kHChunks = 16;   // column chunks of the H sum (summed in order afterwards)
+
+// Hp[z][k][j] = sum over columns of chunk z of aqsn[k][ig] M_2[j][ig]:
+// both rows of pair j as the lanes, the band value broadcast.  Grid: x row
+// pair blocks, y band blocks, z column chunks.
+__global__ void __launch_bounds__(kThreads, 2) mg_gemm_h_kernel(int nbands, int pairs, int nc,
+                                                                int chunk,
+                                                                const float4 *__restrict__ M2,
+                                                                const float4 *__restrict__ band,
+                                                                float4 *__restrict__ Hp) {
+    __shared__ float4 sA[kStep][kPairs][2];
+    __shared__ float4 sB[kStep][kHBands];
+    const int tid = threadIdx.x;
+    const int pr = tid / (kThreads / kPairs), cg = tid % (kThreads / kPairs);
+    const int pair0 = blockIdx.x * kPairs, band0 = blockIdx.y * kHBands;
+    const int ig_begin = blockIdx.z * chunk, ig_end = min(nc, ig_begin + chunk);
+    const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    df2 accr[kPerThread], acci[kPerThread];
+#pragma unroll
+    for (int t = 0; t < kPerThread; ++t) accr[t] = acci[t] = z;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kStep) {
+        const int kc = min(kStep, ig_end - ig0);
+        __syncthreads();
+        for (int i = tid; i < kStep * kPairs * 2; i += kThreads) {
+            const int pp = i / (kStep * 2), c = (i / kStep) % 2, kk = i % kStep;
+            float4 v = zero4;
+            if (kk < kc && pair0 + pp < pairs)
+                v = M2[((size_t)(pair0 + pp) * 2 + c) * nc + ig0 + kk];
+            sA[kk][pp][c] = v;
+        }
+        for (int i = tid; i < kStep * kHBands; i += kThreads) {
+            const int bb = i / kStep, kk = i % kStep;
+            float4 v = zero4;
+            if (kk < kc && band0 + bb < nbands) v = band[(size_t)(band0 + bb) * nc + ig0 + kk];
+            sB[kk][bb] = v;
+        }
+        __syncthreads();
+        for (int kk = 0; kk < kc; ++kk) {
+            const float4 a4 = sA[kk][pr][0], b4 = sA[kk][pr][1];
+            const df2 ar = {f2(a4.x, a4.y), f2(a4.z, a4.w)};
+            const df2 ai = {f2(b4.x, b4.y), f2(b4.z, b4.w)};
+#pragma unroll
+            for (int t = 0; t < kPerThread; ++t) {
+                const float4 v = sB[kk][cg + t * (kThreads / kPairs)];
+                const df2 br = df2_bcast(df{v.x, v.y}), bi = df2_bcast(df{v.z, v.w});
+                accr[t] = df2_sub(df2_add(accr[t], df2_mul(ar, br)), df2_mul(ai, bi));
+                acci[t] = df2_add(df2_add(acci[t], df2_mul(ar, bi)), df2_mul(ai, br));
+            }
+        }
+    }
+    const int j = pair0 + pr;
+    if (j >= pairs) return;
+#pragma unroll
+    for (int t = 0; t < kPerThread; ++t) {
+        const int k = band0 + cg + t * (kThreads / kPairs);
+        if (k >= nbands) continue;
+        float4 *o = Hp + (((size_t)blockIdx.z * nbands + k) * pairs + j) * 2;
+        o[0] = make_float4(accr[t].h.x, accr[t].h.y, accr[t].l.x, accr[t].l.y);
+        o[1] = make_float4(acci[t].h.x, acci[t].h.y, acci[t].l.x, acci[t].l.y);
+    }
+}
+
+// acht_n1_loc partials: band b0 + k, row tile j: sum_rows c H with H the
+// chunk sums of Hp added in chunk order.
+__global__ void __launch_bounds__(kThreads) mg_n1_kernel(Partials part, int b0, int K, int pairs,
+                                                         int chunks, const float4 *cpl,
+                                                         const float4 *Hp) {
+    const long long n = (long long)K * pairs;
+    const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
+    for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (long long)gridDim.x * kThreads) {
+        const int k = (int)(i / pairs), j = (int)(i % pairs);
+        df2 hr = z, hi = z;
+        for (int c = 0; c < chunks; ++c) {
+            const float4 *h = Hp + (((size_t)c * K + k) * pairs + j) * 2;
+            const float4 a = h[0], b = h[1];
+            hr = df2_add(hr, df2{f2(a.x, a.y), f2(a.z, a.w)});
+            hi = df2_add(hi, df2{f2(b.x, b.y), f2(b.z, b.w)});
+        }
+        const float4 a = cpl[i * 2], b = cpl[i * 2 + 1];
+        const df2 cr = {f2(a.x, a.y), f2(a.z, a.w)}, ci = {f2(b.x, b.y), f2(b.z, b.w)};
+        const df2 pr = df2_sub(df2_mul(cr, hr), df2_mul(ci, hi));
+        const df2 pi = df2_add(df2_mul(cr, hi), df2_mul(ci, hr));
+        part.n1[(long long)(b0 + k) * part.n1_seg + j] =
+            make_double2(to_double(df2_lane(pr, 0)) + to_double(df2_lane(pr, 1)),
+                         to_double(df2_lane(pi, 0)) + to_double(df2_lane(pi, 1)));
+    }
+}
+
 int grid_for(long long n) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -238,9 +377,13 @@ float4 *planes_g(const Problem &p, void *ws, int K) {
 
 }  // namespace
 
-size_t mixed_gemm_bytes(const Problem &p, int bands) {
-    return align_up(sizeof(float4) * 2 * (size_t)bands * row_pairs(p)) +
-           align_up(sizeof(float4) * 2 * (size_t)row_pairs(p) * p.nc);
+size_t mixed_gemm_bytes(const Problem &p, int bands, bool want_n1) {
+    size_t b = align_up(sizeof(float4) * 2 * (size_t)bands * row_pairs(p)) +
+               align_up(sizeof(float4) * 2 * (size_t)row_pairs(p) * p.nc);
+    if (want_n1)
+        b += align_up(sizeof(float4) * 2 * (size_t)row_pairs(p) * p.nc) +
+             align_up(sizeof(float4) * 2 * (size_t)kHChunks * bands * row_pairs(p));
+    return b;
 }
 
 gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *split_ws, void *ws,
@@ -280,6 +423,36 @@ gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_w
         default: e = launch_freq_t<8>(p, part, s, b0, G, rt, st); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "mg_freq_kernel");
+    return GPP_OK;
+}
+
+gpp_status mixed_gemm_per_band(const Problem &p, const Partials &part, void *split_ws, void *ws,
+                               int b0, int b1, cudaStream_t st) {
+    const int K = b1 - b0, pairs = row_pairs(p);
+    if (K <= 0 || pairs <= 0 || !part.n1) return GPP_OK;
+    const SplitPlanes s = split_planes_at(p, split_ws);
+    const size_t plane = align_up(sizeof(float4) * 2 * (size_t)pairs * p.nc);
+    float4 *M2 = reinterpret_cast<float4 *>(reinterpret_cast<char *>(planes_g(p, ws, K)) + plane);
+    float4 *Hp = reinterpret_cast<float4 *>(reinterpret_cast<char *>(M2) + plane);
+    mg_m2_kernel<<<grid_for((long long)pairs * p.nc), kThreads, 0, st>>>(p, s, b0, M2);
+    count_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_m2_kernel");
+    const int chunk = ceil_div(ceil_div(p.nc, kHChunks), kStep) * kStep;
+    const int chunks = ceil_div(p.nc, chunk);
+    if (ceil_div(K, kHBands) > 65535)
+        return set_error(GPP_ERR_UNSUPPORTED, "too many bands for the per-band product grid");
+    dim3 grid((unsigned)ceil_div(pairs, kPairs), (unsigned)ceil_div(K, kHBands), (unsigned)chunks);
+    mg_gemm_h_kernel<<<grid, kThreads, 0, st>>>(K, pairs, p.nc, chunk, M2,
+                                                s.band + (size_t)b0 * p.nc, Hp);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_gemm_h_kernel");
+    mg_n1_kernel<<<grid_for((long long)K * pairs), kThreads, 0, st>>>(part, b0, K, pairs, chunks,
+                                                                      planes_c(ws), Hp);
+    count_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_n1_kernel");
     return GPP_OK;
 }
 

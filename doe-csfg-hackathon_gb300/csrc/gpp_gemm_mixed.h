@@ -13,18 +13,22 @@
 namespace gpp {
 
 // Workspace bytes for `bands` unoccupied bands.
-size_t mixed_gemm_bytes(const Problem &p, int bands);
+size_t mixed_gemm_bytes(const Problem &p, int bands, bool want_n1);
 
-// Unoccupied bands [b0, b1) of a problem with wx_stride == 0, achtemp only
-// (no per-band output), on the float-float split planes at `split_ws`
-// (bands and wx split for [b0, b1), rows split before mixed_gemm_rows reads
-// them):
+// Unoccupied bands [b0, b1) of a problem with wx_stride == 0 on the
+// float-float split planes at `split_ws` (bands and wx split for [b0, b1),
+// rows split before mixed_gemm_rows reads them):
 //  1. mixed_gemm_band_sum: c and G = sum_n1 c aqsn over every G' row;
 //  2. mixed_gemm_rows: for row tiles `rows`, each row tile's achtemp partial
-//     (slot part.ach_tile0 + row tile).
+//     (slot part.ach_tile0 + row tile);
+//  3. mixed_gemm_per_band: when part.n1 is set (nw >= 3), the per-band
+//     partials of acht_n1_loc -- H = aqsn M_2^T in float-float over every
+//     row (needs every row split).
 gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *split_ws, void *ws,
                                int b0, int b1, cudaStream_t st);
 gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_ws, void *ws, int b0,
                            int b1, cudaStream_t st, RowTiles rows = RowTiles());
+gpp_status mixed_gemm_per_band(const Problem &p, const Partials &part, void *split_ws, void *ws,
+                               int b0, int b1, cudaStream_t st);
 
 }  // namespace gpp

@@ -105,12 +105,12 @@ def test_gemm_path_through_the_host_pieces(ngpown):
 MIXED_TOL = 1e-8
 
 
-def mixed_with(mode, d, semantics):
+def mixed_with(mode, d, semantics, n1=False):
     from gppsigma import ops
     lib = capi.load()
     capi.check(lib.gpp_set_gemm_path(mode), "gemm path")
     try:
-        r = ops.sigma(d, "mixed", semantics, acht_n1=False, achstemp=False)
+        r = ops.sigma(d, "mixed", semantics, acht_n1=n1, achstemp=False)
         ops.wait()
     finally:
         capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
@@ -129,28 +129,33 @@ def test_mixed_gemm_path_within_1e8_of_fp64(shape, semantics):
     """The float-float band-sum GEMM against the FP64 per-term kernel."""
     from gppsigma import ops
     d = ops.DeviceInputs.from_host(band_independent(shape, 93))
-    m = mixed_with(1, d, semantics)
-    f = sigma_with(0, d, semantics, False)
-    t = mixed_with(0, d, semantics)
+    n1 = shape.nw >= 3
+    m = mixed_with(1, d, semantics, n1)
+    f = sigma_with(0, d, semantics, n1)
+    t = mixed_with(0, d, semantics, n1)
     for key in ("achtemp", "asxtemp"):
         a = getattr(m, key).cpu().numpy()
         assert rel_err(a, getattr(f, key).cpu().numpy()) <= MIXED_TOL, key
         assert rel_err(a, getattr(t, key).cpu().numpy()) <= MIXED_TOL, key
+    if n1:  # per-band output (norm-wise: single bands cancel more than the sums)
+        a, w = m.acht_n1_loc.cpu().numpy(), f.acht_n1_loc.cpu().numpy()
+        assert np.max(np.abs(a - w)) <= MIXED_TOL * np.max(np.abs(w))
 
 
 def test_mixed_gemm_path_through_the_host_pieces():
     from gppsigma import ops
     inp = band_independent(W.Shape(48, 2, 900, 33, 3, near_pole=0.02), 19)
     d = ops.DeviceInputs.from_host(inp)
-    dev = mixed_with(1, d, "complex_seq")
+    dev = mixed_with(1, d, "complex_seq", True)
     arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
                                            "vcoul", "inv_igp_index", "indinv", "wx_array")}
     lib = capi.load()
     capi.check(lib.gpp_set_gemm_path(1), "gemm path")
     try:
         with ops.HostContext() as ctx:
-            host = ctx.sigma(arrays, inp.shape, "mixed")
+            host = ctx.sigma(arrays, inp.shape, "mixed", acht_n1=True)
     finally:
         capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
     assert np.array_equal(host["achtemp"], dev.achtemp.cpu().numpy())
     assert np.array_equal(host["asxtemp"], dev.asxtemp.cpu().numpy())
+    assert np.array_equal(host["acht_n1_loc"], dev.acht_n1_loc.cpu().numpy())
