@@ -12,7 +12,9 @@
 // frequency pass reads it exactly as the per-term kernel reads aqsn * Q:
 // terms within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs
 // and G.  Compared with the per-term kernel the division runs once per
-// (row, column, frequency) instead of once per band.
+// (row, column, frequency) instead of once per band.  The per-band output
+// acht_n1_loc is a second product of the same form, H = aqsn M_2^T, with
+// its long sum over columns split into chunks that are added in order.
 #include "gpp_gemm_mixed.h"
 #include "gpp_tiles_mixed.cuh"
 

@@ -141,8 +141,7 @@ int gpp_get_dropin_precision(void);
  * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM:
  * cuBLAS in FP64, a float-float GEMM on the FP32 pipes in mixed precision),
  * several times faster; the results agree with the per-term kernels to
- * their rounding.  Mixed-precision calls that ask for acht_n1_loc keep the
- * per-term kernel. */
+ * their rounding. */
 gpp_status gpp_set_gemm_path(int mode);
 
 /* ------------------------------------------------------------------------
