@@ -46,6 +46,8 @@ def sigma_with(mode, d, semantics, n1):
     (W.Shape(33, 5, 640, 8, 5, igp_overflow=2), "kerseq"),
     (W.Shape(64, 3, 2048, 64, 8, dw=0.25), "complex_seq"),
     (W.Shape(20, 4, 300, 1, 3), "kerseq"),
+    (W.Shape(40, 2, 1, 1, 3), "complex_seq"),
+    (W.Shape(6, 5, 35, 3, 2), "complex_seq"),
 ])
 def test_gemm_path_equals_per_term_kernel_and_oracle(shape, semantics):
     import oracle_py
@@ -124,6 +126,9 @@ def mixed_with(mode, d, semantics, n1=False):
     (W.Shape(64, 3, 2048, 64, 8, dw=0.25, near_pole=0.02), "complex_seq"),
     (W.Shape(20, 4, 300, 1, 3), "kerseq"),
     (W.Shape(150, 2, 4100, 70, 3, near_pole=0.01), "complex_seq"),
+    (W.Shape(40, 2, 1, 1, 3), "complex_seq"),
+    (W.Shape(6, 5, 35, 3, 2), "kerseq"),
+    (W.Shape(300, 0, 4099, 5, 4, near_pole=0.05), "complex_seq"),
 ])
 def test_mixed_gemm_path_within_1e8_of_fp64(shape, semantics):
     """The float-float band-sum GEMM against the FP64 per-term kernel."""
