@@ -72,6 +72,15 @@ def test_invalid_arguments_are_reported_without_a_device(lib):
     assert lib.gpp_sigma_batched(None, None, -1, None) == capi.GPP_ERR_INVALID_ARGUMENT
 
 
+def test_path_and_precision_setters_validate(lib):
+    assert lib.gpp_set_gemm_path(2) == capi.GPP_ERR_INVALID_ARGUMENT
+    assert lib.gpp_set_gemm_path(-2) == capi.GPP_ERR_INVALID_ARGUMENT
+    for mode in (1, 0, -1):
+        assert lib.gpp_set_gemm_path(mode) == capi.GPP_OK
+    assert lib.gpp_set_dropin_precision(3) == capi.GPP_ERR_INVALID_ARGUMENT
+    assert lib.gpp_set_dropin_precision(-1) == capi.GPP_OK
+
+
 def test_stream_setter_round_trip(lib):
     assert lib.gpp_set_stream(C.c_void_p(0x1234)) == capi.GPP_OK
     assert lib.gpp_get_stream() == 0x1234
