@@ -226,9 +226,7 @@ int dropin_precision() {
 // automatically from 32 unoccupied bands on (below that the per-term kernel
 // is as fast), or as gpp_set_gemm_path forces.
 constexpr int kGemmMinBands = 32;
-bool gemm_path(int precision, int wx_stride, int bands, bool want_n1) {
-    (void)precision;
-    (void)want_n1;
+bool gemm_path(int wx_stride, int bands) {
     if (wx_stride != 0 || bands <= 0) return false;
     return t_gemm_path < 0 ? bands >= kGemmMinBands : t_gemm_path == 1;
 }
@@ -292,7 +290,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const TileShape fs = flag_shape(p);  // same tiling for the FP64 and the mixed occupied tile
     const TileShape ns = mixed ? mixed_noflag_shape(p) : fp64_noflag_shape(p);
     const bool want_n1 = o.n1 && p.nw >= 3 && p.ng > 0;
-    const bool gemm = has_noflag && gemm_path(precision, p.wx_stride, nb1 - nb0, want_n1);
+    const bool gemm = has_noflag && gemm_path(p.wx_stride, nb1 - nb0);
     const long long rows_f = has_flag ? ceil_div(p.ng, fs.rg) : 0;
     const long long rows_n = has_noflag ? ceil_div(p.ng, ns.rg) : 0;
     const long long tiles_f = has_flag ? rows_f * (fb1 - fb0) : 0;
