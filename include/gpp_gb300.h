@@ -124,7 +124,8 @@ gpp_stream_t gpp_get_stream(void);
 /* No counterpart in the reference.  Arithmetic of the drop-in entry points
  * above except gpp_reduce_achstemp (per host thread): GPP_PRECISION_FP64
  * (the reference's) or GPP_PRECISION_MIXED (float-float, <= 1e-8 of FP64,
- * several times faster); -1 restores the process default, which is
+ * about 4x faster for the reference's call sequence); -1 restores the
+ * process default, which is
  * GPP_PRECISION_MIXED when the environment has GPP_DROPIN_PRECISION=mixed
  * and GPP_PRECISION_FP64 otherwise -- so an unmodified reference driver can
  * run the mixed kernels.  gpp_get_dropin_precision returns the value in
