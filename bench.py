@@ -12,8 +12,10 @@ headline runs the mixed-precision kernel and the line also carries the FP64
 kernel's rate and the mixed-vs-FP64 error on the same inputs.
 
 Prints ONE JSON line on rank 0.  With --impl reference it times the
-reference's CPU algorithm (the OpenMP loop shape of gppOpenMP3.cpp, restated
-in oracle/) on all host cores over a bounded band sample of the same workload.
+reference's own OpenMP program (gppOpenMP3.cpp, unmodified, compiled on this
+host by oracle/build_oracle.py) on all host cores over a bounded band sample
+of the same workload shape; where that program cannot run, the oracle's
+restatement of its loop.
 
 Under torchrun (N > 1) every rank runs its own independent state (weak
 scaling, no data-path collective); value = all ranks' terms / max rank time.
@@ -136,9 +138,75 @@ def profile_pipe(kernel_file: str, metric: str):
     return None
 
 
-def run_reference(args, shape: W.Shape) -> dict:
-    """CPU baseline: the reference's OpenMP loop (gppOpenMP3.cpp:278-333)
-    restated in oracle/, all host threads, a bounded band sample per step."""
+def _reference_line(args, shape, value, ms, cores, kind, sample) -> dict:
+    return {"metric": METRIC, "value": value, "unit": "terms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)" if kind == "port" else
+                    "the reference program's own ramp inputs (its timing does not depend on values)",
+            "impl": "reference",
+            "config": {"workload": args.workload, **shape_dict(shape)},
+            "cpu_baseline": {"value": value, "unit": "terms/s", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+_TIME_RE = re.compile(r"Time Taken \*+= *([0-9.eE+-]+) *secs")
+
+
+def _run_program(exe: str, nb: int, nv: int, nc: int, npg: int, threads: int) -> float:
+    """One run of the reference's OpenMP program; returns its own loop time (s)."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    out = subprocess.run([exe, str(nb), str(nv), str(nc), str(npg)], capture_output=True,
+                         text=True, env=env, timeout=600, check=True).stdout
+    m = _TIME_RE.search(out)
+    if not m:
+        raise RuntimeError("no timing line in the reference program's output")
+    return float(m.group(1))
+
+
+def run_reference_program(args, shape: W.Shape):
+    """CPU baseline: the reference's unmodified OpenMP program (gppOpenMP3.cpp,
+    its loop gppOpenMP3.cpp:274-336 timed by its own gettimeofday), built on
+    this host by oracle/build_oracle.py, all host threads.  It takes argv
+    `number_bands nvband ncouls nodes_per_group` (ngpown = ncouls /
+    nodes_per_group) and 3 frequencies, so it covers workloads of that form;
+    each step runs a band sample sized to ~ref_seconds.  None when the
+    program is not available here or the workload is not of that form."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import build_oracle
+    exe = build_oracle.build_openmp_reference()
+    if exe is None or shape.nw != 3 or shape.ngpown == 0:
+        return None
+    npg = shape.ncouls // shape.ngpown
+    if npg < 1 or shape.ncouls // npg != shape.ngpown:
+        return None
+    cores = os.cpu_count() or 1
+    nv, nc, ng = shape.nvband, shape.ncouls, shape.ngpown
+    # Calibrate on a few unoccupied bands, then size the sample.
+    probe = nv + 8
+    t = _run_program(exe, probe, nv, nc, npg, cores)
+    per_band = max(t / probe, 1e-4)
+    nb = int(max(nv + 1, min(shape.number_bands, args.ref_seconds / per_band)))
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt = _run_program(exe, nb, nv, nc, npg, cores)
+        if i >= args.warmup:
+            times.append(dt)
+    terms = nb * ng * nc * 3
+    ms = 1e3 * statistics.mean(times)
+    value = terms / (ms * 1e-3)
+    sample = (f"the unmodified reference program gppOpenMP3 (OpenMP, {cores} threads), argv "
+              f"'{nb} {nv} {nc} {npg}': bands 0..{nb - 1} of the workload's shape "
+              f"({terms:.3e} terms per step), its own loop timer")
+    return _reference_line(args, shape, value, ms, cores, "reference", sample)
+
+
+def run_reference_port(args, shape: W.Shape) -> dict:
+    """CPU baseline where the reference program cannot run: its OpenMP loop
+    (gppOpenMP3.cpp:278-333) restated in oracle/, all host threads, a bounded
+    band sample per step."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle_py
 
@@ -165,17 +233,21 @@ def run_reference(args, shape: W.Shape) -> dict:
     terms = samp.shape.terms
     ms = 1e3 * statistics.mean(times)
     value = terms / (ms * 1e-3)
-    sample = (f"bands 0..{samp.shape.number_bands - 1} ({shape.nvband} occupied + {nb_sample} "
+    sample = (f"oracle restatement of the reference's OpenMP loop, bands "
+              f"0..{samp.shape.number_bands - 1} ({shape.nvband} occupied + {nb_sample} "
               f"unoccupied) of the workload: {terms:.3e} terms per step")
-    return {"metric": METRIC, "value": value, "unit": "terms/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": args.workload, **shape_dict(shape)},
-            "cpu_baseline": {"value": value, "unit": "terms/s", "cores": cores, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+    return _reference_line(args, shape, value, ms, cores, "port", sample)
+
+
+def run_reference(args, shape: W.Shape) -> dict:
+    """The reference arm: the reference's own OpenMP program where it runs on
+    this host, else the oracle's restatement of its loop."""
+    line = None
+    try:
+        line = run_reference_program(args, shape)
+    except (subprocess.SubprocessError, RuntimeError, OSError) as e:
+        print(f"reference program failed ({e}); timing the oracle port", file=sys.stderr)
+    return line if line is not None else run_reference_port(args, shape)
 
 
 def shape_dict(s: W.Shape) -> dict:
@@ -274,7 +346,8 @@ def main() -> int:
                     choices=sorted(W.CONFIGS) + sorted(BATCHED))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-seconds", type=float, default=4.0,
+                    help="CPU seconds per step of the reference arm's band sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--shard", default="states", choices=["states", "rows"],
                     help="states: one independent state per rank (weak scaling); rows: one "

@@ -62,12 +62,15 @@ gpp_status cuda_fail(cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-// One persistent fault word per device (allocated on first use).
+// One persistent fault word and one workspace pool per device (created on
+// first use).  The pool is the library's own: workspace allocations stay
+// cached between calls (release threshold: never), and the caller's
+// default pool and its settings are left untouched.
 std::mutex g_dev_mutex;
 int *g_err_word[256] = {};
-bool g_pool_ready[256] = {};
+cudaMemPool_t g_pool[256] = {};
 
-gpp_status device_setup(int *dev_out, int **err_out) {
+gpp_status device_setup(int *dev_out, int **err_out, cudaMemPool_t *pool_out = nullptr) {
     int dev = 0;
     GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= 256) return fail(GPP_ERR_UNSUPPORTED, "device ordinal %d", dev);
@@ -78,68 +81,36 @@ gpp_status device_setup(int *dev_out, int **err_out) {
         GPP_CUDA_TRY(cudaMemset(w, 0, sizeof(int)), "cudaMemset(fault word)");
         g_err_word[dev] = w;
     }
-    if (!g_pool_ready[dev]) {
-        // Keep stream-ordered workspace allocations cached between calls.
-        cudaMemPool_t pool;
-        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-            unsigned long long thr = ~0ull;
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    if (!g_pool[dev]) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        GPP_CUDA_TRY(cudaMemPoolCreate(&pool, &props), "cudaMemPoolCreate(workspace pool)");
+        unsigned long long thr = ~0ull;
+        cudaError_t e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(pool);
+            return cuda_fail(e, "cudaMemPoolSetAttribute(workspace pool)");
         }
-        g_pool_ready[dev] = true;
+        g_pool[dev] = pool;
     }
     *dev_out = dev;
     *err_out = g_err_word[dev];
+    if (pool_out) *pool_out = g_pool[dev];
     return GPP_OK;
 }
 
-bool mul_ok(long long a, long long b, long long lim) { return a == 0 || b <= lim / a; }
-
-gpp_status validate(const gpp_problem *pr) {
-    if (!pr) return fail(GPP_ERR_INVALID_ARGUMENT, "problem is NULL");
-    const gpp_problem &p = *pr;
-    if (p.number_bands < 0 || p.nvband < 0 || p.nvband > p.number_bands)
-        return fail(GPP_ERR_INVALID_ARGUMENT, "need 0 <= nvband <= number_bands (got %d, %d)",
-                    p.nvband, p.number_bands);
-    if (p.ncouls <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ncouls must be > 0 (got %d)", p.ncouls);
-    if (p.ngpown < 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ngpown must be >= 0 (got %d)", p.ngpown);
-    if (p.nw <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "nw must be > 0 (got %d)", p.nw);
-    if (p.wx_stride != 0 && p.wx_stride < p.nw)
-        return fail(GPP_ERR_INVALID_ARGUMENT, "wx_stride must be 0 or >= nw (got %d)", p.wx_stride);
-    if (p.semantics != GPP_SEM_COMPLEX_SEQ && p.semantics != GPP_SEM_KERSEQ)
-        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown semantics %d", p.semantics);
-    if (p.precision != GPP_PRECISION_FP64 && p.precision != GPP_PRECISION_MIXED)
-        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown precision %d", p.precision);
-    const long long lim = (long long)1 << 60;
-    if (!mul_ok(p.number_bands, p.ncouls, lim) || !mul_ok(p.ngpown, p.ncouls, lim) ||
-        !mul_ok((long long)p.number_bands * (p.wx_stride ? 1 : 0), p.wx_stride ? p.wx_stride : 1, lim))
-        return fail(GPP_ERR_INVALID_ARGUMENT, "array sizes overflow");
-    if (p.number_bands > 0 && (!p.aqsmtemp || !p.aqsntemp))
-        return fail(GPP_ERR_INVALID_ARGUMENT, "aqsmtemp/aqsntemp is NULL");
-    if (p.ngpown > 0 && (!p.I_eps_array || !p.wtilde_array || !p.inv_igp_index))
-        return fail(GPP_ERR_INVALID_ARGUMENT, "I_eps_array/wtilde_array/inv_igp_index is NULL");
-    if (!p.vcoul || !p.wx_array) return fail(GPP_ERR_INVALID_ARGUMENT, "vcoul/wx_array is NULL");
+// Stream-ordered workspace from the library's pool of the current device.
+gpp_status workspace_alloc(void **ptr, size_t bytes, cudaStream_t s) {
+    int dev = 0;
+    int *err = nullptr;
+    cudaMemPool_t pool = nullptr;
+    gpp_status st = device_setup(&dev, &err, &pool);
+    if (st != GPP_OK) return st;
+    GPP_CUDA_TRY(cudaMallocFromPoolAsync(ptr, bytes, pool, s), "cudaMallocFromPoolAsync(workspace)");
     return GPP_OK;
-}
-
-Problem to_problem(const gpp_problem &q) {
-    Problem p;
-    p.aqsm = reinterpret_cast<const double2 *>(q.aqsmtemp);
-    p.aqsn = reinterpret_cast<const double2 *>(q.aqsntemp);
-    p.ieps = reinterpret_cast<const double2 *>(q.I_eps_array);
-    p.wt = reinterpret_cast<const double2 *>(q.wtilde_array);
-    p.vcoul = q.vcoul;
-    p.inv_igp = q.inv_igp_index;
-    p.indinv = q.indinv;
-    p.wx = q.wx_array;
-    p.wx_stride = q.wx_stride;
-    p.nb = q.number_bands;
-    p.nv = q.nvband;
-    p.nc = q.ncouls;
-    p.ng = q.ngpown;
-    p.nw = q.nw;
-    p.occ = q.occ;
-    p.semantics = q.semantics;
-    return p;
 }
 
 // Where the final fixed-order sums go.
@@ -297,10 +268,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     // The GEMM path writes one partial per row tile (all bands at once).
     const long long tiles_n =
         !has_noflag ? 0 : gemm ? rows_n : rows_n * ceil_div(nb1 - nb0, ns.rn);
-    if (has_noflag && !gemm && ceil_div(nb1 - nb0, ns.rn) > 65535)
-        return fail(GPP_ERR_UNSUPPORTED, "too many bands for one launch (%d)", nb1 - nb0);
-    if (ceil_div(p.nw, ns.nwc) > 65535 || (has_flag && fb1 - fb0 > 65535))
-        return fail(GPP_ERR_UNSUPPORTED, "too many frequencies or occupied bands");
+    st = check_grid_limits(p, has_flag ? fb1 - fb0 : 0, has_noflag ? nb1 - nb0 : 0, ns, gemm);
+    if (st != GPP_OK) return st;
     if (has_flag && fb0 != 0)
         return fail(GPP_ERR_UNSUPPORTED, "occupied-band launches start at band 0");
     const long long ach_seg = tiles_f + tiles_n;
@@ -320,7 +289,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const size_t ws_bytes = off > 0 ? off : 256;
 
     void *ws = nullptr;
-    GPP_CUDA_TRY(cudaMallocAsync(&ws, ws_bytes, s), "cudaMallocAsync(workspace)");
+    st = workspace_alloc(&ws, ws_bytes, s);
+    if (st != GPP_OK) return st;
     char *w = static_cast<char *>(ws);
 
     Partials part{};
@@ -433,6 +403,68 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
 }
 
 }  // namespace
+
+static bool mul_ok(long long a, long long b, long long lim) { return a == 0 || b <= lim / a; }
+
+gpp_status validate(const gpp_problem *pr) {
+    if (!pr) return fail(GPP_ERR_INVALID_ARGUMENT, "problem is NULL");
+    const gpp_problem &p = *pr;
+    if (p.number_bands < 0 || p.nvband < 0 || p.nvband > p.number_bands)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "need 0 <= nvband <= number_bands (got %d, %d)",
+                    p.nvband, p.number_bands);
+    if (p.ncouls <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ncouls must be > 0 (got %d)", p.ncouls);
+    if (p.ngpown < 0) return fail(GPP_ERR_INVALID_ARGUMENT, "ngpown must be >= 0 (got %d)", p.ngpown);
+    if (p.nw <= 0) return fail(GPP_ERR_INVALID_ARGUMENT, "nw must be > 0 (got %d)", p.nw);
+    if (p.wx_stride != 0 && p.wx_stride < p.nw)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "wx_stride must be 0 or >= nw (got %d)", p.wx_stride);
+    if (p.semantics != GPP_SEM_COMPLEX_SEQ && p.semantics != GPP_SEM_KERSEQ)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown semantics %d", p.semantics);
+    if (p.precision != GPP_PRECISION_FP64 && p.precision != GPP_PRECISION_MIXED)
+        return fail(GPP_ERR_INVALID_ARGUMENT, "unknown precision %d", p.precision);
+    const long long lim = (long long)1 << 60;
+    if (!mul_ok(p.number_bands, p.ncouls, lim) || !mul_ok(p.ngpown, p.ncouls, lim) ||
+        !mul_ok((long long)p.number_bands * (p.wx_stride ? 1 : 0), p.wx_stride ? p.wx_stride : 1, lim))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "array sizes overflow");
+    if (p.number_bands > 0 && (!p.aqsmtemp || !p.aqsntemp))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "aqsmtemp/aqsntemp is NULL");
+    if (p.ngpown > 0 && (!p.I_eps_array || !p.wtilde_array || !p.inv_igp_index))
+        return fail(GPP_ERR_INVALID_ARGUMENT, "I_eps_array/wtilde_array/inv_igp_index is NULL");
+    if (!p.vcoul || !p.wx_array) return fail(GPP_ERR_INVALID_ARGUMENT, "vcoul/wx_array is NULL");
+    return GPP_OK;
+}
+
+Problem to_problem(const gpp_problem &q) {
+    Problem p;
+    p.aqsm = reinterpret_cast<const double2 *>(q.aqsmtemp);
+    p.aqsn = reinterpret_cast<const double2 *>(q.aqsntemp);
+    p.ieps = reinterpret_cast<const double2 *>(q.I_eps_array);
+    p.wt = reinterpret_cast<const double2 *>(q.wtilde_array);
+    p.vcoul = q.vcoul;
+    p.inv_igp = q.inv_igp_index;
+    p.indinv = q.indinv;
+    p.wx = q.wx_array;
+    p.wx_stride = q.wx_stride;
+    p.nb = q.number_bands;
+    p.nv = q.nvband;
+    p.nc = q.ncouls;
+    p.ng = q.ngpown;
+    p.nw = q.nw;
+    p.occ = q.occ;
+    p.semantics = q.semantics;
+    return p;
+}
+
+// Grid limits of one call's launches: grid.y of the unoccupied-band kernels
+// counts band tiles, grid.y of the occupied-band kernels counts occupied
+// bands, grid.z counts frequency chunks; each must stay <= 65535.
+gpp_status check_grid_limits(const Problem &p, int occupied_bands, int unoccupied_bands,
+                             const TileShape &ns, bool gemm) {
+    if (unoccupied_bands > 0 && !gemm && ceil_div(unoccupied_bands, ns.rn) > 65535)
+        return fail(GPP_ERR_UNSUPPORTED, "too many bands for one launch (%d)", unoccupied_bands);
+    if (ceil_div(p.nw, ns.nwc) > 65535 || occupied_bands > 65535)
+        return fail(GPP_ERR_UNSUPPORTED, "too many frequencies or occupied bands");
+    return GPP_OK;
+}
 
 int tuned_mixed_variant(int dev, int nw) { return mixed_variant_for(dev, nw); }
 
@@ -901,7 +933,8 @@ gpp_status gpp_autotune(const gpp_problem *problem, int max_bands, gpp_stream_t 
     int dev = 0;
     GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     double2 *out = nullptr;
-    GPP_CUDA_TRY(cudaMallocAsync(&out, sizeof(double2) * 2 * (size_t)p.nw, s), "cudaMallocAsync");
+    st = workspace_alloc(reinterpret_cast<void **>(&out), sizeof(double2) * 2 * (size_t)p.nw, s);
+    if (st != GPP_OK) return st;
     OutSpec o;
     o.ach = out;
     o.asx = out + p.nw;

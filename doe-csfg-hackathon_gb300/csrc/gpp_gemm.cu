@@ -10,18 +10,27 @@
 //   G[r][ig]    = sum_{n1 >= nvband} c[n1][r] aqsn[n1][ig],
 //   c[n1][r]    = 0.5 vcoul[igp(r)] conj(aqsm[n1][igp(r)]),
 //
-// G is one complex GEMM over the bands (cuBLAS cublasZgemm3m: the 3M form,
-// three real FP64 GEMMs instead of four, 187 ms against 231 ms for
-// cublasZgemm at the production shape on GB300; FP64 complex has no tcgen05
-// form), and a fused pass over (r, ig) builds M on the fly and sums M G per
-// row tile -- the same block-partial slots and fixed-order reduction as the
-// per-term kernels.  The per-band output acht_n1_loc (iw = 2) needs
+// G is one complex GEMM over the bands, and a fused pass over (r, ig) builds
+// M on the fly and sums M G per row tile -- the same block-partial slots and
+// fixed-order reduction as the per-term kernels.  The per-band output
+// acht_n1_loc (iw = 2) needs
 //   acht_n1_loc[n1] = sum_r c[n1][r] H[n1][r],  H[n1][r] = sum_ig aqsn[n1][ig] M_2[r][ig],
 // a second GEMM against M_2 stored once.  Exact in real arithmetic; only
-// the order of the FP64 roundings differs from the per-term kernel (and the
-// 3M form's own, within ~1e-15 of the sums here).
-#include <cublas_v2.h>
-
+// the order of the FP64 roundings differs from the per-term kernel.
+//
+// Both GEMMs are zgemm3m_kernel below, written for GB300's FP64 pipe (no
+// library): complex products in the 3M form (Gauss's three real products:
+// re = P1 - P2, im = P3 - P1 - P2 with P1 = sum xr yr, P2 = sum xi yi,
+// P3 = sum (xr + xi)(yr + yi)), so one complex multiply-add costs three
+// DFMAs instead of four.  GB300 retires ~2 DFMA per clock per SM and no
+// faster FP64 form exists on it (its FP64 tensor rate is the same), so the
+// kernel is built to keep that pipe busy and nothing else: register tiles of
+// 4 x 2 outputs per thread, operands staged through shared memory as three
+// planes (re, im, re + im -- the sums formed once per staged element, not
+// once per product), two blocks per SM so that one stages while the other
+// computes.  Shared-memory and HBM traffic are a few percent of the DFMA
+// time.  Each output sums its k range in increasing k in one thread, and
+// split-k partials are added in split order: the results are bit-reproducible.
 #include <algorithm>
 #include <cstdio>
 
@@ -43,27 +52,140 @@ gpp_status cuda_fail(cudaError_t e, const char *what) {
 
 constexpr int kThreads = 256;
 
-struct Handle {
-    int dev = -1;
-    cublasHandle_t h = nullptr;
-};
-thread_local Handle t_blas;
+// ---------------------------------------------------------------------------
+// zgemm3m_kernel: Out[m][n] = sum_{k in split} X(m, k) Y(n, k), complex FP64.
+// X(m, k) = X[m * xs + k] when XKFast, else X[k * xs + m]; Y likewise.  Block
+// tile kBM x kBN outputs, kBK k values per shared-memory stage; thread
+// (tx, ty) of a 16 x 16 grid owns rows ty + 16 i (i < kTM) and columns
+// tx + 16 j (j < kTN), so its shared-memory reads are broadcasts or runs of
+// consecutive words.  blockIdx.z is the k split: it covers
+// [z * k_per_split, min(K, (z + 1) * k_per_split)) and writes its partial at
+// Out + z * split_stride.
+constexpr int kBM = 64, kBN = 32, kBK = 32, kTM = 4, kTN = 2, kGThreads = 256;
+constexpr int kXP = kBM + 1, kYP = kBN + 1;  // padded plane rows
+constexpr size_t kGemmSmem = sizeof(double) * 3 * kBK * (kXP + kYP);
 
-cublasStatus_t blas_handle(cudaStream_t s, cublasHandle_t *out) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (t_blas.dev != dev) {
-        if (t_blas.h) cublasDestroy(t_blas.h);
-        t_blas.h = nullptr;
-        t_blas.dev = -1;
-        cublasStatus_t st = cublasCreate(&t_blas.h);
-        if (st != CUBLAS_STATUS_SUCCESS) return st;
-        t_blas.dev = dev;
+template <bool XKFast, bool YKFast>
+__global__ void __launch_bounds__(kGThreads, 2)
+zgemm3m_kernel(const double2 *__restrict__ X, long long xs, const double2 *__restrict__ Y,
+               long long ys, double2 *__restrict__ Out, long long out_ld, long long split_stride,
+               int M, int N, int K, int k_per_split) {
+    extern __shared__ double smem[];
+    double *xr = smem, *xi = xr + kBK * kXP, *xsum = xi + kBK * kXP;
+    double *yr = xsum + kBK * kXP, *yi = yr + kBK * kYP, *ysum = yi + kBK * kYP;
+    const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
+    const int kb = blockIdx.z * k_per_split;
+    const int ke = min(K, kb + k_per_split);
+    double p1[kTM][kTN], p2[kTM][kTN], p3[kTM][kTN];
+#pragma unroll
+    for (int i = 0; i < kTM; ++i)
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) p1[i][j] = p2[i][j] = p3[i][j] = 0.0;
+
+    for (int k0 = kb; k0 < ke; k0 += kBK) {
+        // Stage X (kBM x kBK) and Y (kBN x kBK) as re / im / re+im planes,
+        // zero outside the matrix; reads are coalesced along the unit stride.
+#pragma unroll 4
+        for (int e = t; e < kBM * kBK; e += kGThreads) {
+            const int k = XKFast ? e % kBK : e / kBM, m = XKFast ? e / kBK : e % kBM;
+            double2 v = make_double2(0.0, 0.0);
+            if (m0 + m < M && k0 + k < ke)
+                v = __ldg(X + (XKFast ? (long long)(m0 + m) * xs + (k0 + k)
+                                      : (long long)(k0 + k) * xs + (m0 + m)));
+            xr[k * kXP + m] = v.x;
+            xi[k * kXP + m] = v.y;
+            xsum[k * kXP + m] = v.x + v.y;
+        }
+#pragma unroll 4
+        for (int e = t; e < kBN * kBK; e += kGThreads) {
+            const int k = YKFast ? e % kBK : e / kBN, n = YKFast ? e / kBK : e % kBN;
+            double2 v = make_double2(0.0, 0.0);
+            if (n0 + n < N && k0 + k < ke)
+                v = __ldg(Y + (YKFast ? (long long)(n0 + n) * ys + (k0 + k)
+                                      : (long long)(k0 + k) * ys + (n0 + n)));
+            yr[k * kYP + n] = v.x;
+            yi[k * kYP + n] = v.y;
+            ysum[k * kYP + n] = v.x + v.y;
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int k = 0; k < kBK; ++k) {
+            double ar[kTM], ai[kTM], as[kTM], br[kTN], bi[kTN], bs[kTN];
+#pragma unroll
+            for (int i = 0; i < kTM; ++i) {
+                ar[i] = xr[k * kXP + ty + 16 * i];
+                ai[i] = xi[k * kXP + ty + 16 * i];
+                as[i] = xsum[k * kXP + ty + 16 * i];
+            }
+#pragma unroll
+            for (int j = 0; j < kTN; ++j) {
+                br[j] = yr[k * kYP + tx + 16 * j];
+                bi[j] = yi[k * kYP + tx + 16 * j];
+                bs[j] = ysum[k * kYP + tx + 16 * j];
+            }
+#pragma unroll
+            for (int i = 0; i < kTM; ++i)
+#pragma unroll
+                for (int j = 0; j < kTN; ++j) {
+                    p1[i][j] = fma(ar[i], br[j], p1[i][j]);
+                    p2[i][j] = fma(ai[i], bi[j], p2[i][j]);
+                    p3[i][j] = fma(as[i], bs[j], p3[i][j]);
+                }
+        }
+        __syncthreads();
     }
-    cublasStatus_t st = cublasSetStream(t_blas.h, s);
-    *out = t_blas.h;
-    return st;
+    double2 *out = Out + (long long)blockIdx.z * split_stride;
+#pragma unroll
+    for (int i = 0; i < kTM; ++i) {
+        const int m = m0 + ty + 16 * i;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < kTN; ++j) {
+            const int n = n0 + tx + 16 * j;
+            if (n < N)
+                out[(long long)m * out_ld + n] =
+                    make_double2(p1[i][j] - p2[i][j], p3[i][j] - p1[i][j] - p2[i][j]);
+        }
+    }
 }
+
+// k values per split when a K-long sum is cut `splits` ways: split
+// boundaries fall on kBK multiples, so every stage but a split's last is full.
+int zgemm_k_per_split(int K, int splits) { return ceil_div(ceil_div(K, splits), kBK) * kBK; }
+// Number of non-empty splits that makes (<= splits).
+int zgemm_splits(int K, int splits) { return ceil_div(K, zgemm_k_per_split(K, splits)); }
+
+// Launches zgemm3m_kernel over an M x N output with zgemm_splits(K, splits)
+// k splits, split z written at Out + z * split_stride.
+template <bool XKFast, bool YKFast>
+cudaError_t launch_zgemm3m(const double2 *X, long long xs, const double2 *Y, long long ys,
+                           double2 *Out, long long out_ld, long long split_stride, int M, int N,
+                           int K, int splits, cudaStream_t s) {
+    static bool configured[256] = {};  // the attribute is set per device
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (!configured[dev & 255]) {
+        e = cudaFuncSetAttribute(zgemm3m_kernel<XKFast, YKFast>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
+        if (e != cudaSuccess) return e;
+        configured[dev & 255] = true;
+    }
+    const int per = zgemm_k_per_split(K, splits);
+    const int z = ceil_div(K, per);
+    if (ceil_div(M, kBM) > 65535 || z > 65535)
+        return cudaErrorInvalidConfiguration;
+    dim3 grid((unsigned)ceil_div(N, kBN), (unsigned)ceil_div(M, kBM), (unsigned)z);
+    zgemm3m_kernel<XKFast, YKFast><<<grid, kGThreads, kGemmSmem, s>>>(
+        X, xs, Y, ys, Out, out_ld, split_stride, M, N, K, per);
+    count_launch();
+    return cudaGetLastError();
+}
+
+// k splits of the per-band GEMM (H = aqsn M_2^T sums over all ncouls
+// columns): enough blocks for ~10 waves of two blocks per SM.
+constexpr int kHSplits = 8;
 
 // c[k][r] for bands b0 + k (k < K) and rows [r0, r1); rows whose G' index
 // is invalid get 0 (their fault bit is set, as in the per-term epilogue).
@@ -160,11 +282,14 @@ __global__ void __launch_bounds__(kThreads) gemm_m2_kernel(Problem p, int r0, in
 }
 
 // acht_n1_loc partials: band b0 + k, row tile j: sum over the tile's rows of
-// c[k][r] H[k][r].
+// c[k][r] H[k][r], H being the sum of the per-band GEMM's k splits (added in
+// split order).
 __global__ void __launch_bounds__(kThreads) gemm_n1_kernel(Problem p, Partials part, int b0,
                                                            int K, int tile0, int tiles,
-                                                           const double2 *C, const double2 *H) {
+                                                           const double2 *C, const double2 *H,
+                                                           int splits) {
     const long long n = (long long)K * tiles;
+    const size_t split_stride = (size_t)K * p.ng;
     for (long long i = (long long)blockIdx.x * kThreads + threadIdx.x; i < n;
          i += (long long)gridDim.x * kThreads) {
         const int k = (int)(i / tiles), j = tile0 + (int)(i % tiles);
@@ -173,7 +298,9 @@ __global__ void __launch_bounds__(kThreads) gemm_n1_kernel(Problem p, Partials p
             const int r = 2 * j + g;
             if (r >= p.ng) continue;
             const size_t at = (size_t)k * p.ng + r;
-            tot = cadd(tot, cmul(C[at], H[at]));
+            double2 h = H[at];
+            for (int z = 1; z < splits; ++z) h = cadd(h, H[z * split_stride + at]);
+            tot = cadd(tot, cmul(C[at], h));
         }
         part.n1[(long long)(b0 + k) * part.n1_seg + j] = tot;
     }
@@ -199,18 +326,14 @@ cudaError_t launch_epilogue_t(const Problem &p, const Partials &part, const doub
     return cudaGetLastError();
 }
 
-gpp_status blas_fail(cublasStatus_t st, const char *what) {
-    char buf[256];
-    snprintf(buf, sizeof(buf), "%s failed (cuBLAS status %d)", what, (int)st);
-    return set_error(st == CUBLAS_STATUS_ALLOC_FAILED ? GPP_ERR_OUT_OF_MEMORY : GPP_ERR_CUDA, buf);
-}
 
 }  // namespace
 
 size_t gemm_bytes(const Problem &p, int bands, bool want_n1) {
     const size_t k = (size_t)bands, ng = (size_t)p.ng, nc = (size_t)p.nc;
     size_t b = align_up(sizeof(double2) * k * ng) + align_up(sizeof(double2) * ng * nc);
-    if (want_n1) b += align_up(sizeof(double2) * ng * nc) + align_up(sizeof(double2) * k * ng);
+    if (want_n1)
+        b += align_up(sizeof(double2) * ng * nc) + align_up(sizeof(double2) * kHSplits * k * ng);
     return b;
 }
 
@@ -236,8 +359,6 @@ GemmBuffers carve(const Problem &p, void *ws, int K, bool want_n1) {
     return b;
 }
 
-const cuDoubleComplex kOne = {1.0, 0.0}, kZero = {0.0, 0.0};
-
 }  // namespace
 
 gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
@@ -250,16 +371,10 @@ gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_coeff_kernel");
-    cublasHandle_t h = nullptr;
-    cublasStatus_t bs = blas_handle(s, &h);
-    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasCreate/cublasSetStream");
-    // Column-major view: aqsn rows are columns of an (nc x K) matrix, C of an
-    // (ng x K) one, G of an (nc x ng) one: G = aqsn * C^T.
-    bs = cublasZgemm3m(h, CUBLAS_OP_N, CUBLAS_OP_T, p.nc, p.ng, K, &kOne,
-                     reinterpret_cast<const cuDoubleComplex *>(p.aqsn + (size_t)b0 * p.nc), p.nc,
-                     reinterpret_cast<const cuDoubleComplex *>(b.C), p.ng, &kZero,
-                     reinterpret_cast<cuDoubleComplex *>(b.G), p.nc);
-    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasZgemm (band sum)");
+    // G (ng x nc) = C^T aqsn: X(r, k) = C[k][r], Y(ig, k) = aqsn[b0 + k][ig].
+    e = launch_zgemm3m<false, false>(b.C, p.ng, p.aqsn + (size_t)b0 * p.nc, p.nc, b.G, p.nc, 0,
+                                     p.ng, p.nc, K, 1, s);
+    if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (band sum)");
     return GPP_OK;
 }
 
@@ -289,18 +404,15 @@ gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
-    cublasHandle_t h = nullptr;
-    cublasStatus_t bs = blas_handle(s, &h);
-    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasCreate/cublasSetStream");
-    // H (column-major ng x K) = M_2^T * aqsn.
-    bs = cublasZgemm3m(h, CUBLAS_OP_T, CUBLAS_OP_N, p.ng, K, p.nc, &kOne,
-                     reinterpret_cast<const cuDoubleComplex *>(b.M2), p.nc,
-                     reinterpret_cast<const cuDoubleComplex *>(p.aqsn + (size_t)b0 * p.nc), p.nc,
-                     &kZero, reinterpret_cast<cuDoubleComplex *>(b.H), p.ng);
-    if (bs != CUBLAS_STATUS_SUCCESS) return blas_fail(bs, "cublasZgemm (per-band output)");
+    // H (K x ng) = aqsn M_2^T: X(k', ig) = aqsn[b0 + k'][ig], Y(r, ig) = M_2[r][ig],
+    // the ncouls sum split kHSplits ways.
+    e = launch_zgemm3m<true, true>(p.aqsn + (size_t)b0 * p.nc, p.nc, b.M2, p.nc, b.H, p.ng,
+                                   (long long)K * p.ng, K, p.ng, p.nc, kHSplits, s);
+    if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (per-band output)");
     const int tiles = ceil_div(p.ng, 2);
     gemm_n1_kernel<<<grid_for((long long)K * tiles), kThreads, 0, s>>>(p, part, b0, K, 0, tiles,
-                                                                       b.C, b.H);
+                                                                       b.C, b.H,
+                                                                       zgemm_splits(p.nc, kHSplits));
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_n1_kernel");

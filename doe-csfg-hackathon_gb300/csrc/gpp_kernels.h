@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include "gpp_gb300.h"
 #include "gpp_internal.cuh"
 
 namespace gpp {
@@ -100,6 +101,16 @@ struct BatchItem {
 
 // Pipeline variant of the mixed kernel chosen for (device, nw).
 int tuned_mixed_variant(int dev, int nw);
+
+// Argument checks shared by every entry point (gpp_api.cu): sizes, pointers,
+// enum values and size overflow; on failure they record the message for
+// gpp_last_error_message.
+gpp_status validate(const gpp_problem *problem);
+Problem to_problem(const gpp_problem &q);
+// Grid limits of one call's launches (occupied bands, unoccupied band tiles,
+// frequency chunks), GPP_ERR_UNSUPPORTED beyond them.
+gpp_status check_grid_limits(const Problem &p, int occupied_bands, int unoccupied_bands,
+                             const TileShape &ns, bool gemm);
 
 // Per-thread launch counter (gpp_launch_count).
 void count_launch(int n = 1);

@@ -80,42 +80,19 @@ using namespace gpp;
 
 extern "C" gpp_status gpp_sigma_static_scratch(const gpp_problem *problem, const gpp_outputs *out,
                                                gpp_stream_t stream) {
-    if (!problem || !out) return set_error(GPP_ERR_INVALID_ARGUMENT, "problem/outputs is NULL");
-    const gpp_problem &q = *problem;
-    if (q.number_bands < 0 || q.nvband < 0 || q.nvband > q.number_bands || q.ncouls <= 0 ||
-        q.ngpown < 0 || q.nw <= 0 || (q.wx_stride != 0 && q.wx_stride < q.nw))
-        return set_error(GPP_ERR_INVALID_ARGUMENT, "invalid sizes");
-    if (q.semantics != GPP_SEM_COMPLEX_SEQ && q.semantics != GPP_SEM_KERSEQ)
-        return set_error(GPP_ERR_INVALID_ARGUMENT, "unknown semantics");
-    if (q.precision != GPP_PRECISION_FP64)
+    if (!out) return set_error(GPP_ERR_INVALID_ARGUMENT, "outputs is NULL");
+    // The same argument checks as gpp_sigma: sizes, pointers, enum values,
+    // size overflow.
+    gpp_status st = validate(problem);
+    if (st != GPP_OK) return st;
+    if (problem->precision != GPP_PRECISION_FP64)
         return set_error(GPP_ERR_UNSUPPORTED, "gpp_sigma_static_scratch computes in FP64 only");
     if (!out->achtemp || !out->asxtemp)
         return set_error(GPP_ERR_INVALID_ARGUMENT, "outputs achtemp/asxtemp are required");
     if (out->acht_n1_loc || out->achstemp)
         return set_error(GPP_ERR_UNSUPPORTED,
                          "gpp_sigma_static_scratch returns achtemp and asxtemp only");
-    if ((q.number_bands > 0 && (!q.aqsmtemp || !q.aqsntemp)) ||
-        (q.ngpown > 0 && (!q.I_eps_array || !q.wtilde_array || !q.inv_igp_index)) || !q.vcoul ||
-        !q.wx_array)
-        return set_error(GPP_ERR_INVALID_ARGUMENT, "an input array is NULL");
-
-    Problem p;
-    p.aqsm = reinterpret_cast<const double2 *>(q.aqsmtemp);
-    p.aqsn = reinterpret_cast<const double2 *>(q.aqsntemp);
-    p.ieps = reinterpret_cast<const double2 *>(q.I_eps_array);
-    p.wt = reinterpret_cast<const double2 *>(q.wtilde_array);
-    p.vcoul = q.vcoul;
-    p.inv_igp = q.inv_igp_index;
-    p.indinv = q.indinv;
-    p.wx = q.wx_array;
-    p.wx_stride = q.wx_stride;
-    p.nb = q.number_bands;
-    p.nv = q.nvband;
-    p.nc = q.ncouls;
-    p.ng = q.ngpown;
-    p.nw = q.nw;
-    p.occ = q.occ;
-    p.semantics = q.semantics;
+    const Problem p = to_problem(*problem);
 
     // Block-partial layout, as gpp_sigma uses it: achtemp partials of the
     // occupied then unoccupied blocks, then asxtemp partials.
@@ -125,8 +102,10 @@ extern "C" gpp_status gpp_sigma_static_scratch(const gpp_problem *problem, const
     const long long tiles_f = has_flag ? (long long)ceil_div(p.ng, fs.rg) * p.nv : 0;
     const long long tiles_n =
         has_noflag ? (long long)ceil_div(p.ng, ns.rg) * ceil_div(p.nb - p.nv, ns.rn) : 0;
-    if (has_noflag && ceil_div(p.nb - p.nv, ns.rn) > 65535)
-        return set_error(GPP_ERR_UNSUPPORTED, "too many bands for one launch");
+    // The grid limits of gpp_sigma's launches (this entry point never takes
+    // the band-sum GEMM path).
+    st = check_grid_limits(p, has_flag ? p.nv : 0, has_noflag ? p.nb - p.nv : 0, ns, false);
+    if (st != GPP_OK) return st;
     const size_t ach_bytes = align256(sizeof(double2) * (size_t)((tiles_f + tiles_n) * p.nw));
     const size_t need = ach_bytes + align256(sizeof(double2) * (size_t)(tiles_f * p.nw));
     if (need > kStaticScratchBytes) {
@@ -139,7 +118,7 @@ extern "C" gpp_status gpp_sigma_static_scratch(const gpp_problem *problem, const
 
     void *scratch = nullptr;
     int *fault = nullptr;
-    gpp_status st = static_addresses(&scratch, &fault);
+    st = static_addresses(&scratch, &fault);
     if (st != GPP_OK) return st;
 
     Partials part{};

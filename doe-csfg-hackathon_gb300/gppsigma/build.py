@@ -78,11 +78,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 f.result()
     lib_objs = [os.path.join(OBJDIR, n + ".o") for n in LIB_SOURCES]
     if force or _stale(LIB, lib_objs):
-        # cuBLAS (the band-independent FP64 path's ZGEMM) from the toolkit
-        # that compiles the library, found at run time through the rpath.
-        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(_nvcc()))), "lib64")
-        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *lib_objs, "-lcublas",
-               "-Xlinker", f"-rpath,{cudalib}"]
+        # Every kernel is this library's own: it links the CUDA runtime only.
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *lib_objs]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

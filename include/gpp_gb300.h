@@ -203,10 +203,16 @@ gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compu
 /* No counterpart in the reference.  gpp_sigma for callers that cannot
  * allocate device memory -- applications that have handed the GPU's memory
  * to their own arena or to another runtime, or that cannot afford
- * cudaMalloc's device-wide synchronisation mid-step.  It runs the same FP64
- * kernels as gpp_sigma but keeps the block partials in a fixed 8 MiB array in
- * the library's device image (resident on every GPU that loads the library),
- * so it allocates nothing.  FP64 only; achtemp and asxtemp only (acht_n1_loc
+ * cudaMalloc's device-wide synchronisation mid-step.  It always runs the
+ * per-term FP64 kernels and keeps their block partials in a fixed 8 MiB array
+ * in the library's device image (resident on every GPU that loads the
+ * library), so it allocates nothing.  With per-band wx (wx_stride > 0), or
+ * fewer than 32 unoccupied bands, those are gpp_sigma's own kernels and the
+ * results are bit-identical; with band-independent wx and 32 or more
+ * unoccupied bands gpp_sigma sums the bands as a GEMM instead, and the two
+ * agree to FP64 rounding (1e-12 relative), not bit for bit, the per-term
+ * kernels being the slower of the two there.  The argument checks and grid
+ * limits are gpp_sigma's.  FP64 only; achtemp and asxtemp only (acht_n1_loc
  * and achstemp must be NULL); problems needing more than 8 MiB of partials
  * (the production shape needs ~5 MiB) return GPP_ERR_UNSUPPORTED.  All calls
  * share the array: calls whose GPU work overlaps in time race, so serialise

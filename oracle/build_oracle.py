@@ -12,6 +12,12 @@ Two products:
     - ``libref_kerseq.so``:      gppKerSeq.cpp      + ref_harness.cpp
     - ``gppKerSeq.ex``, ``gppComplex_seq.ex``, ``gppOpenMP3.ex``: the
       unmodified reference executables (README known-answer runs, CPU timing).
+    - ``src/gppOpenMP3.cpp``: an untracked copy of the reference's OpenMP
+      program, a single self-contained source file, staged here so that a
+      host without the reference checkout (the GPU host, an aarch64 machine
+      that cannot run the x86 executable built here) compiles the unmodified
+      program itself (``build_openmp_reference``) for bench.py's reference
+      arm.  oracle/_ref/ is git-ignored: nothing of the reference is committed.
     - ``GPPComplex.cubin`` and ``gppCuda.cubin``: the device code of the
       reference's two CUDA versions (GPPComplex.cu, called by gppCudaVer.cpp;
       gppCuda.cu, the unified-memory one) for sm_103a, loaded by
@@ -31,7 +37,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF_DIR = "/root/reference"
+# The reference checkout (read-only); GPP_REFERENCE_DIR overrides the default.
+DEFAULT_REF_DIR = os.environ.get("GPP_REFERENCE_DIR", "/root/reference")
+STAGE = os.path.join(REF_OUT, "src")
+OPENMP_EX = os.path.join(REF_OUT, "gppOpenMP3.ex")
 
 ORACLE_SO = os.path.join(BUILD, "libgpp_oracle.so")
 
@@ -78,6 +87,10 @@ def build_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool
         if force or _stale(target, [srcp, harness]):
             _run(common + ["-shared", "-D" + macro, "-Dmain=gpp_reference_unused_main",
                            srcp, harness, "-o", target])
+    os.makedirs(STAGE, exist_ok=True)
+    staged = os.path.join(STAGE, "gppOpenMP3.cpp")
+    if force or _stale(staged, [os.path.join(ref_dir, "gppOpenMP3.cpp")]):
+        shutil.copyfile(os.path.join(ref_dir, "gppOpenMP3.cpp"), staged)
     exes = [("gppKerSeq.ex", "gppKerSeq.cpp", []),
             ("gppComplex_seq.ex", "gppComplex_seq.cpp", []),
             ("gppOpenMP3.ex", "gppOpenMP3.cpp", ["-fopenmp"])]
@@ -88,6 +101,39 @@ def build_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool
             _run(["g++", "-O3", "-w", "-I", ref_dir] + extra + [srcp, "-o", target])
     build_reference_cubin(ref_dir, force)
     return True
+
+
+def build_openmp_reference(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> str | None:
+    """Compile the reference's unmodified OpenMP program (gppOpenMP3.cpp, with
+    the reference's own -O3 -fopenmp) into oracle/_ref/gppOpenMP3.ex, from the
+    checkout when present, else from the staged copy in oracle/_ref/src/.
+    Returns the executable's path, or None when neither source is here or
+    the host has no OpenMP compiler."""
+    src = os.path.join(ref_dir, "gppOpenMP3.cpp")
+    if not os.path.isfile(src):
+        src = os.path.join(STAGE, "gppOpenMP3.cpp")
+    if not os.path.isfile(src):
+        return OPENMP_EX if _runs(OPENMP_EX) else None
+    if force or _stale(OPENMP_EX, [src]) or not _runs(OPENMP_EX):
+        os.makedirs(REF_OUT, exist_ok=True)
+        try:
+            _run(["g++", "-O3", "-w", "-fopenmp", src, "-o", OPENMP_EX + ".tmp"])
+        except (subprocess.CalledProcessError, OSError):
+            return None
+        os.replace(OPENMP_EX + ".tmp", OPENMP_EX)
+    return OPENMP_EX
+
+
+def _runs(exe: str) -> bool:
+    """Whether `exe` exists and runs on this host (it prints its usage line
+    and exits when given no arguments)."""
+    if not os.path.isfile(exe):
+        return False
+    try:
+        subprocess.run([exe], capture_output=True, timeout=30)
+        return True
+    except (OSError, subprocess.TimeoutExpired):
+        return False
 
 
 def build_reference_cubin(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -> bool:
@@ -117,6 +163,8 @@ def build_reference_cubin(ref_dir: str = DEFAULT_REF_DIR, force: bool = False) -
 def main() -> int:
     build_oracle(force="--force" in sys.argv)
     ok = build_reference(force="--force" in sys.argv)
+    omp = build_openmp_reference(force="--force" in sys.argv)
+    print("reference OpenMP program:", omp or "not available on this host")
     print("oracle:", ORACLE_SO)
     print("reference:", REF_OUT if ok else "not present on this machine")
     return 0

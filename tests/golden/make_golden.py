@@ -10,7 +10,15 @@ machine, without the reference checkout.
 The ramp cases are the reference's own known-answer inputs; their README
 values (README.md:26-41, 15 significant digits) are stored as published.
 
-    python tests/golden/make_golden.py      # needs the reference checkout
+    python tests/golden/make_golden.py         # needs the reference checkout
+    python tests/golden/make_golden.py --full  # the production shapes, ~6 min each
+
+``--full`` writes tests/golden/gpp_golden_full.json: the benchmark's own
+workloads at full size (number_bands 512, nvband 2, ncouls 32768, ngpown 1638,
+3 frequencies, seed 20240607; with and without 1% near-pole wtilde), summed
+by the reference's functions (one thread, ~5 min per shape) and by the C
+restatement on all host threads; the two must agree bit for bit before the
+fixture is written.
 """
 from __future__ import annotations
 
@@ -65,11 +73,48 @@ def hexlist(a):
     return [[float(z.real).hex(), float(z.imag).hex()] for z in a]
 
 
+OUT_FULL = os.path.join(HERE, "gpp_golden_full.json")
+# The benchmark's workloads and seed (bench.py).
+FULL = [("production", 20240607), ("production_near_pole", 20240607)]
+
+
+def main_full() -> int:
+    """Full-size fixtures: the reference's functions and the oracle on the
+    benchmark's own inputs, required to agree bit for bit."""
+    cases = []
+    for name, seed in FULL:
+        shape = W.CONFIGS[name]
+        inp = W.make_inputs(shape, seed)
+        digest = inp.digest()
+        ref = oracle_py.run(inp, "complex_seq", impl="ref_complex_seq")
+        orc = oracle_py.run(inp, "complex_seq", impl="oracle", nthreads=oracle_py.max_threads())
+        for key in ("achtemp", "asxtemp", "acht_n1_loc", "achstemp"):
+            if hexlist(ref[key]) != hexlist(orc[key]):
+                print(f"{name}: oracle and reference differ in {key}", file=sys.stderr)
+                return 1
+        cases.append({"name": name, "kind": "seeded", "shape": dataclasses.asdict(shape),
+                      "seed": seed, "semantics": "complex_seq", "digest": digest,
+                      "achtemp": hexlist(ref["achtemp"]), "asxtemp": hexlist(ref["asxtemp"]),
+                      "acht_n1_loc": hexlist(ref["acht_n1_loc"]),
+                      "achstemp": hexlist(ref["achstemp"]),
+                      "oracle_bit_exact": True})
+        print(name, "done", flush=True)
+    with open(OUT_FULL, "w") as f:
+        json.dump({"generator": "tests/golden/make_golden.py --full",
+                   "source": "reference functions gppComplex_seq.cpp via oracle/ref_harness.cpp; "
+                             "oracle/gpp_oracle.c gives the same bits",
+                   "cases": cases}, f, indent=1)
+    print("wrote", OUT_FULL, len(cases), "cases")
+    return 0
+
+
 def main() -> int:
     build_oracle.build_oracle()
     if not build_oracle.build_reference():
         print("reference checkout not found; fixtures not regenerated", file=sys.stderr)
         return 1
+    if "--full" in sys.argv:
+        return main_full()
     cases = []
     for (nb, nv, nc, npg), readme in README.items():
         inp = W.ramp_inputs(nb, nv, nc, npg)

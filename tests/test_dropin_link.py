@@ -9,7 +9,11 @@ import pytest
 
 from gppsigma import build
 
-REF = "/root/reference"
+# The reference checkout, read-only (oracle/build_oracle.py resolves
+# GPP_REFERENCE_DIR the same way).
+import build_oracle  # noqa: E402
+
+REF = build_oracle.DEFAULT_REF_DIR
 
 
 @pytest.mark.skipif(not os.path.isfile(os.path.join(REF, "gppCudaVer.cpp")),

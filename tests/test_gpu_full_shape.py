@@ -1,0 +1,85 @@
+"""The benchmark's own workloads at full size against the reference's outputs.
+
+tests/golden/gpp_golden_full.json holds achtemp, asxtemp, achstemp and the
+per-band acht_n1_loc that the reference's sequential functions
+(gppComplex_seq.cpp, driven by oracle/ref_harness.cpp over the loop nest of
+gppComplex_seq.cpp:335-383) computed on the production shape (number_bands
+512, nvband 2, ncouls 32768, ngpown 1638, 3 frequencies, 8.24e10 terms;
+seed 20240607), with and without 1% near-pole wtilde.  The C oracle gave the
+same bits when the fixture was written.  Here the inputs are generated on the
+GPU exactly as bench.py generates them; their sha256 must equal the fixture's,
+and then:
+
+* the FP64 path is within 1e-12 per real/imaginary component;
+* the mixed-precision path is within 1e-8 (the headline's bound), and within
+  1e-10 (what the float-float kernels deliver with margin).
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import REPO, rel_err, unhex
+from gppsigma import build, capi, workload as W
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+FP64_TOL = 1e-12
+MIXED_TOL = 1e-8
+MIXED_DELIVERED = 1e-10
+FULL = os.path.join(REPO, "tests", "golden", "gpp_golden_full.json")
+
+
+def _cases():
+    with open(FULL) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    build.build()
+    capi.load()
+
+
+def device_digest(d) -> str:
+    """sha256 of the device inputs in workload.Inputs.digest()'s order."""
+    h = hashlib.sha256()
+    for t in (d.aqsmtemp, d.aqsntemp, d.I_eps_array, d.wtilde_array, d.vcoul, d.inv_igp_index,
+              d.indinv, d.wx_array):
+        h.update(t.contiguous().cpu().numpy().tobytes())
+    return h.hexdigest()
+
+
+def norm_err(got, want) -> float:
+    """Max abs error over the array relative to the array's max modulus (the
+    per-band sums cancel more than the totals)."""
+    return float(np.max(np.abs(got - want)) / max(np.max(np.abs(want)), 1e-300))
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: c["name"])
+def test_full_production_shape_matches_reference(case):
+    from gppsigma import ops as o
+    shape = W.Shape(**case["shape"])
+    d = o.device_inputs(shape, case["seed"])
+    assert device_digest(d) == case["digest"], "device generator drifted from the fixture's inputs"
+    want = {k: unhex(case[k]) for k in ("achtemp", "asxtemp", "achstemp", "acht_n1_loc")}
+    errs = {}
+    for precision, tol in (("fp64", FP64_TOL), ("mixed", MIXED_DELIVERED)):
+        r = o.sigma(d, precision, acht_n1=True, achstemp=True)
+        o.wait()
+        e = {k: rel_err(getattr(r, k).cpu().numpy(), want[k]) for k in ("achtemp", "asxtemp")}
+        e["acht_n1_loc"] = norm_err(r.acht_n1_loc.cpu().numpy(), want["acht_n1_loc"])
+        errs[precision] = e
+        for k, v in e.items():
+            assert v <= tol, f"{precision} {k}: {v:.3e} > {tol:g}"
+            assert v <= (FP64_TOL if precision == "fp64" else MIXED_TOL)
+        # The static term is FP64 in both precisions.
+        assert rel_err(r.achstemp.cpu().numpy(), want["achstemp"]) <= FP64_TOL
+    print(case["name"], json.dumps(errs))
+    del d
+    torch.cuda.empty_cache()

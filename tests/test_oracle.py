@@ -114,3 +114,20 @@ def test_extended_oracle_sees_a_planted_error():
     inp.aqsntemp[7, 100] *= 1 + 1e-9
     b = oracle_py.run(inp, impl="oracle_extended", nthreads=4)
     assert np.max(np.abs(a["achtemp"] - b["achtemp"])) > 0
+
+
+def test_oracle_matches_full_shape_reference_outputs_per_band():
+    """The full production shape with 1% near-pole wtilde (the benchmark's
+    workload, 8.2e10 terms): its fixture holds the reference's own per-band
+    sums acht_n1_loc.  A band's sum does not depend on the other bands, so
+    the oracle over the first bands (occupied and unoccupied) must give those
+    bands' fixture values bit for bit, and the host generator must give the
+    fixture's inputs."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "gpp_golden_full.json")) as f:
+        case = {c["name"]: c for c in json.load(f)["cases"]}["production_near_pole"]
+    inp = W.make_inputs(W.Shape(**case["shape"]), case["seed"])
+    assert inp.digest() == case["digest"]
+    r = oracle_py.run(inp, case["semantics"], nthreads=oracle_py.max_threads(), band_end=4)
+    want = unhex(case["acht_n1_loc"])[:4]
+    assert np.array_equal(r["acht_n1_loc"][:4], want)
