@@ -51,12 +51,14 @@ FLOPS_PER_TRIPLE = 12.0
 
 def mixed_fp32_ops_per_term(nwc: int) -> float:
     """FP32 operations the mixed kernel issues per unoccupied term, counted
-    from its column routine: per ig column a thread issues 44 packed
-    instructions shared by its frequencies (A = aqsn*Q, A*Im(wtilde),
-    Im(wtilde)^2) and 75 per frequency (wdiff, |wdiff|^2, reciprocal, the two
-    products, the two accumulations), each packed instruction doing one FP32
-    operation for each of the tile's two rows."""
-    return (44.0 + 75.0 * nwc) / nwc
+    from its column routine (the exact-subtraction form every chunk takes
+    when Re(wtilde) and wx lie below 16): per ig column a thread issues 44
+    packed instructions shared by its frequencies (A = aqsn*Q, A*Im(wtilde),
+    Im(wtilde)^2) and 68 per frequency (Re(wdiff) 2 + renormalisation 3,
+    |wdiff|^2 12, reciprocal 3, the two numerators 24, the two products by
+    the reciprocal 8, the two accumulations 16), each packed instruction
+    doing one FP32 operation for each of the tile's two rows."""
+    return (44.0 + 68.0 * nwc) / nwc
 
 
 class ClockSampler:
@@ -136,6 +138,32 @@ def profile_pipe(kernel_file: str, metric: str):
             m = re.search(r"([0-9.]+)\s*%", line)
             return float(m.group(1)) if m else None
     return None
+
+
+FULL_FIXTURES = os.path.join(REPO, "tests", "golden", "gpp_golden_full.json")
+
+
+def errors_vs_reference_outputs(workload: str, seed: int, got: dict):
+    """Max relative error per real/imaginary component of achtemp and asxtemp
+    against the reference's own sequential outputs for this exact workload
+    (tests/golden/gpp_golden_full.json, written by make_golden.py --full; the
+    oracle gives the same bits), or None when no fixture covers it."""
+    import json
+    if not os.path.exists(FULL_FIXTURES):
+        return None
+    with open(FULL_FIXTURES) as f:
+        cases = {c["name"]: c for c in json.load(f)["cases"]}
+    case = cases.get(workload)
+    if case is None or case["seed"] != seed or W.Shape(**case["shape"]) != W.CONFIGS[workload]:
+        return None
+    out = {"fixture": "tests/golden/gpp_golden_full.json:" + workload,
+           "inputs_sha256": case["digest"]}
+    for key in ("achtemp", "asxtemp"):
+        want = np.array([complex(float.fromhex(a), float.fromhex(b)) for a, b in case[key]])
+        g = np.asarray(got[key], dtype=np.complex128)
+        g2, w2 = np.concatenate([g.real, g.imag]), np.concatenate([want.real, want.imag])
+        out[key] = float(np.max(np.abs(g2 - w2) / np.where(w2 == 0, 1.0, np.abs(w2))))
+    return out
 
 
 def _reference_line(args, shape, value, ms, cores, kind, sample) -> dict:
@@ -381,8 +409,8 @@ def main() -> int:
     full_shape = shape
     if args.shard == "rows":
         # One state, G' rows split across the ranks (gppMPIOpenMP3.cpp:171-172).
-        r0, r1 = gdist.row_range(shape.ngpown, rank, ws)
-        d = ops.device_inputs(shape, SEED).rows(r0, r1)
+        # Each rank generates and holds only its rows of I_eps / wtilde.
+        d, (r0, r1) = gdist.rank_rows_inputs(shape, SEED, rank, ws)
         shape = dataclasses.replace(shape, ngpown=r1 - r0)
         job_terms = full_shape.terms
     else:
@@ -447,6 +475,7 @@ def main() -> int:
     clk = clocks.stop()
 
     fp64_leg = None
+    mixed_vs_oracle = None
     if precision == "mixed":
         r64, ms64, k64, _ = timed("fp64", args.fp64_steps, 1)
         a, b = res.achtemp.cpu().numpy(), r64.achtemp.cpu().numpy()
@@ -467,6 +496,16 @@ def main() -> int:
         fp64_leg = {"value": job_terms / (ms64 * 1e-3), "ms_per_step": ms64,
                     "kernel_ms": k64ms,
                     "max_rel_err_mixed_vs_fp64": {"achtemp": rel(a, b), "asxtemp": rel(x, y)}}
+        # Both precisions against the reference's own outputs on these inputs
+        # (rank 0's state is the seeded workload; with --shard rows the sums
+        # above already cover the whole state).
+        seed0 = SEED if args.shard == "rows" else gdist.state_seed(SEED, 0)
+        if rank == 0:
+            vs_ref = errors_vs_reference_outputs(args.workload, seed0, {"achtemp": a, "asxtemp": x})
+            if vs_ref:
+                mixed_vs_oracle = vs_ref
+                fp64_leg["max_rel_err_vs_oracle"] = errors_vs_reference_outputs(
+                    args.workload, seed0, {"achtemp": b, "asxtemp": y})
         if k64ms and fp64_peak:
             # The FP64 kernel against the measured FP64 FMA rate (algorithmic flops).
             a64 = unocc_terms * (FLOPS_PER_TERM_BASE + FLOPS_PER_TRIPLE / shape.nw) / (k64ms * 1e-3)
@@ -563,6 +602,8 @@ def main() -> int:
     if fp64_leg:
         line["fp64"] = fp64_leg
         line["mixed_speedup_vs_fp64"] = line["value"] / fp64_leg["value"]
+    if mixed_vs_oracle:
+        line["max_rel_err_vs_oracle"] = mixed_vs_oracle
     if not args.no_cpu_baseline:
         ref_args = argparse.Namespace(**vars(args))
         ref_args.steps, ref_args.warmup = 1, 0

@@ -243,6 +243,7 @@ struct RowPieces {
     int n = 0;
     int pair[kMaxRowPieces + 1] = {};
     cudaEvent_t ready[kMaxRowPieces] = {};
+    cudaEvent_t started[kMaxRowPieces] = {};  // optional: compute stream passed ready[k]
 };
 
 gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutSpec &o,
@@ -329,6 +330,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         rt.begin = pc.pair[k];
         rt.end = pc.pair[k + 1];
         if (pieces) e = cudaStreamWaitEvent(s, pc.ready[k], 0);
+        if (e == cudaSuccess && pieces && pc.started[k]) e = cudaEventRecord(pc.started[k], s);
         if (e == cudaSuccess && mixed) e = launch_split_rows(p, w + o_split, rt, s);
         if (e == cudaSuccess && overlap) e = cudaEventRecord(side->fork, s);  // planes written
         if (e == cudaSuccess && has_flag && !overlap) {
@@ -725,6 +727,11 @@ struct gpp_context {
     cudaEvent_t ev[5] = {};
     cudaEvent_t bands_ready = nullptr, done = nullptr;
     cudaEvent_t ready[kMaxRowPieces] = {};
+    // Timing twins of the copy milestones (bands landed, piece k landed) and
+    // the compute stream's start of each piece, for gpp_context_last_trace.
+    cudaEvent_t t_bands = nullptr;
+    cudaEvent_t t_ready[kMaxRowPieces] = {}, t_started[kMaxRowPieces] = {};
+    int pieces = 0;
     bool timed = false;
 };
 
@@ -735,11 +742,41 @@ struct gpp_context {
 // the unoccupied-band kernel.
 constexpr int kHostPieceCuts[] = {1, 5, 16};
 
+// The piece cuts in effect: GPP_HOST_PIECES="c1,c2,...,16" (increasing
+// sixteenths ending at 16, at most kMaxRowPieces of them) overrides the
+// default, for hosts whose links move rows at another speed.
+std::vector<int> host_piece_cuts() {
+    static const std::vector<int> cuts = [] {
+        std::vector<int> v;
+        if (const char *env = getenv("GPP_HOST_PIECES")) {
+            int last = 0;
+            for (const char *c = env; *c;) {
+                char *end = nullptr;
+                const long x = strtol(c, &end, 10);
+                if (end == c || x <= last || x > 16) { v.clear(); break; }
+                v.push_back((int)x);
+                last = (int)x;
+                c = (*end == ',') ? end + 1 : end;
+                if (*end && *end != ',') { v.clear(); break; }
+            }
+            if (v.empty() || v.back() != 16 || (int)v.size() > kMaxRowPieces) v.clear();
+        }
+        if (v.empty()) v.assign(std::begin(kHostPieceCuts), std::end(kHostPieceCuts));
+        return v;
+    }();
+    return cuts;
+}
+
 static void context_release(gpp_context *c) {
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto &e : c->ready)
         if (e) cudaEventDestroy(e);
+    for (auto &e : c->t_ready)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : c->t_started)
+        if (e) cudaEventDestroy(e);
+    if (c->t_bands) cudaEventDestroy(c->t_bands);
     if (c->bands_ready) cudaEventDestroy(c->bands_ready);
     if (c->done) cudaEventDestroy(c->done);
     if (c->copy) cudaStreamDestroy(c->copy);
@@ -756,6 +793,9 @@ gpp_status gpp_context_create(gpp_context **ctx) {
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < kMaxRowPieces && e == cudaSuccess; ++i)
         e = cudaEventCreateWithFlags(&c->ready[i], cudaEventDisableTiming);
+    for (int i = 0; i < kMaxRowPieces && e == cudaSuccess; ++i) e = cudaEventCreate(&c->t_ready[i]);
+    for (int i = 0; i < kMaxRowPieces && e == cudaSuccess; ++i) e = cudaEventCreate(&c->t_started[i]);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->t_bands);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->bands_ready, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -819,11 +859,12 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     for (int k : {kVcoul, kInvIgp, kIndinv, kWx, kAqsm, kAqsn})
         if (in[k].bytes) GPP_CUDA_TRY(h2d(k, 0, in[k].bytes), "cudaMemcpyAsync(H2D)");
     GPP_CUDA_TRY(cudaEventRecord(ctx->bands_ready, ctx->copy), "cudaEventRecord");
+    GPP_CUDA_TRY(cudaEventRecord(ctx->t_bands, ctx->copy), "cudaEventRecord");
     RowPieces pieces;
     const int pairs = (int)((ng + 1) / 2);
     pieces.n = 0;
     pieces.pair[0] = 0;
-    for (int cut : kHostPieceCuts) {
+    for (int cut : host_piece_cuts()) {
         const int b = (int)((long long)pairs * cut / 16);
         if (b > pieces.pair[pieces.n]) pieces.pair[++pieces.n] = b;
     }
@@ -836,8 +877,11 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
             GPP_CUDA_TRY(h2d(kIeps, r0 * nc * 16, (r1 - r0) * nc * 16), "cudaMemcpyAsync(H2D)");
         }
         pieces.ready[k] = ctx->ready[k];
+        pieces.started[k] = ctx->t_started[k];
         GPP_CUDA_TRY(cudaEventRecord(ctx->ready[k], ctx->copy), "cudaEventRecord");
+        GPP_CUDA_TRY(cudaEventRecord(ctx->t_ready[k], ctx->copy), "cudaEventRecord");
     }
+    ctx->pieces = pieces.n;
     GPP_CUDA_TRY(cudaEventRecord(ctx->ev[1], ctx->copy), "cudaEventRecord");
 
     gpp_problem q = h;
@@ -892,6 +936,22 @@ gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compu
     if (compute_ms)
         GPP_CUDA_TRY(cudaEventElapsedTime(compute_ms, ctx->ev[2], ctx->ev[3]), "cudaEventElapsedTime");
     if (d2h_ms) GPP_CUDA_TRY(cudaEventElapsedTime(d2h_ms, ctx->ev[3], ctx->ev[4]), "cudaEventElapsedTime");
+    return GPP_OK;
+}
+
+gpp_status gpp_context_last_trace(gpp_context *ctx, float *ms, int capacity, int *count) {
+    if (!ctx || !count) return fail(GPP_ERR_INVALID_ARGUMENT, "ctx/count is NULL");
+    if (!ctx->timed) return fail(GPP_ERR_NOT_READY, "no completed gpp_sigma_host call");
+    const int n = 1 + 2 * ctx->pieces;
+    *count = n;
+    if (!ms || capacity < n) return fail(GPP_ERR_INVALID_ARGUMENT, "trace needs %d floats", n);
+    GPP_CUDA_TRY(cudaEventElapsedTime(&ms[0], ctx->ev[0], ctx->t_bands), "cudaEventElapsedTime");
+    for (int k = 0; k < ctx->pieces; ++k) {
+        GPP_CUDA_TRY(cudaEventElapsedTime(&ms[1 + 2 * k], ctx->ev[0], ctx->t_ready[k]),
+                     "cudaEventElapsedTime");
+        GPP_CUDA_TRY(cudaEventElapsedTime(&ms[2 + 2 * k], ctx->ev[0], ctx->t_started[k]),
+                     "cudaEventElapsedTime");
+    }
     return GPP_OK;
 }
 

@@ -136,4 +136,31 @@ __host__ __device__ __forceinline__ df2 df2_rcp(const df2 &d) {
     return {r, f2mul(r, e)};
 }
 
+// The reciprocal 1/d of df2_rcp in two parts, the seed r0 and the
+// correction factor c = e + e^2 (1/d = r0 (1 + c) to ~2^-45), for
+// df2_mul_rcp: a product by 1/d then needs no separate low part r0 c.
+__host__ __device__ __forceinline__ void df2_rcp_parts(const df2 &d, float2 &r0, float2 &c) {
+#ifdef __CUDA_ARCH__
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.x) : "f"(d.h.x));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0.y) : "f"(d.h.y));
+#else
+    r0 = make_float2(1.0f / d.h.x, 1.0f / d.h.y);
+#endif
+    float2 e = f2fma(f2neg(d.h), r0, f2(1.0f, 1.0f));
+    e = f2fma(f2neg(d.l), r0, e);
+    c = f2fma(e, e, e);
+}
+// a / d = a r0 (1 + c) in df: p = a.h r0 with its exact rounding error, plus
+// the correction p c and the low part a.l r0.  p c stands for a.h r0 c
+// (their difference, 2^-24 of a term already 2^-22 small, is far below the
+// df rounding); four packed instructions, as df2_mul(a, {r0, r0 c}) costs
+// after the extra one that forms r0 c.
+__host__ __device__ __forceinline__ df2 df2_mul_rcp(const df2 &a, float2 r0, float2 c) {
+    const float2 p = f2mul(a.h, r0);
+    float2 e = f2fma(a.h, r0, f2neg(p));
+    e = f2fma(p, c, e);
+    e = f2fma(a.l, r0, e);
+    return {p, e};
+}
+
 }  // namespace gpp

@@ -67,17 +67,20 @@ __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes 
             const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
             const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
             const double2 q1 = cmul(wt1, __ldg(p.ieps + r1 * nc + ig));
-            const df a0 = split_bits(wt0.x), a1 = split_bits(wt1.x);
+            df a0 = split_bits(wt0.x), a1 = split_bits(wt1.x);
             const df b0 = split_bits(wt0.y), b1 = split_bits(wt1.y);
             const df c0 = split_bits(q0.x), c1 = split_bits(q1.x);
             const df d0 = split_bits(q0.y), d1 = split_bits(q1.y);
+            // Buckets of the nearest floats; then Re(wtilde) in coarse/fine
+            // form where it fits (kWideBit marks the chunk otherwise).
+            unsigned long long bits =
+                bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
+            if (!coarse_fine(a0) | !coarse_fine(a1)) bits |= kWideBit;
             float4 *o = s.rows + j * 4 * nc + ig;
             o[0] = make_float4(a0.h, a1.h, a0.l, a1.l);
             o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
             o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
             o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
-            const unsigned long long bits =
-                bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
             const unsigned long long word = j * nmw + ig / kMaskCols;
             const unsigned act = __activemask();
             const unsigned grp = __match_any_sync(act, word);
@@ -101,7 +104,8 @@ __global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes
     const int nwx = (b1 - b0) * p.nw;
     for (int i = blockIdx.x * 256 + threadIdx.x; i < nwx; i += gridDim.x * 256) {
         const int b = b0 + i / p.nw, iw = i % p.nw;
-        const df x = split(__ldg(p.wx + (size_t)b * p.wx_stride + iw));
+        df x = split(__ldg(p.wx + (size_t)b * p.wx_stride + iw));
+        coarse_fine(x);  // (hi, lo) kept for |wx| >= 16
         s.wx[(size_t)b * p.nw + iw] = make_float2(x.h, x.l);
     }
 }

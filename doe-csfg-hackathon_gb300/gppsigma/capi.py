@@ -44,6 +44,7 @@ _SIGS = {
     "gpp_till_nvband": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d]),
     "gpp_noflag_occ_solver": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gpp_reduce_achstemp": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _i, _vp]),
+    "gpp_reduce_achstemp_split": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gpp_set_stream": (_i, [_vp]),
     "gpp_get_stream": (_vp, []),
     "gpp_sigma": (_i, [C.POINTER(GppProblem), C.POINTER(GppOutputs), _vp]),
@@ -69,6 +70,7 @@ _SIGS = {
     "gpp_probe_fma_peaks": (_i, [C.POINTER(_d), C.POINTER(_d)]),
     "gpp_context_last_timing": (_i, [_vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                      C.POINTER(C.c_float)]),
+    "gpp_context_last_trace": (_i, [_vp, C.POINTER(C.c_float), _i, C.POINTER(_i)]),
     "gpp_selftest_wait_timeout": (_i, [_i, _vp]),
     "gpp_set_dropin_precision": (_i, [_i]),
     "gpp_get_dropin_precision": (_i, []),

@@ -29,6 +29,16 @@ def row_range(ngpown: int, rank: int, world: int) -> tuple[int, int]:
     return min(2 * p0, ngpown), min(2 * p1, ngpown)
 
 
+def rank_rows_inputs(shape, seed: int, rank: int, world: int, device="cuda"):
+    """One rank's share of a state sharded by G' rows: rows row_range(...) of
+    I_eps / wtilde / inv_igp_index, generated where they are used, plus the
+    band arrays every rank needs.  The rank holds its rows only (about
+    1/world of the G'-indexed arrays).  Returns (inputs, (r0, r1))."""
+    from . import ops
+    r0, r1 = row_range(shape.ngpown, rank, world)
+    return ops.device_inputs(shape, seed, device=device, rows=(r0, r1)), (r0, r1)
+
+
 def state_seed(base: int, rank: int) -> int:
     """Seed of the independent state a rank runs."""
     return base + 1000003 * rank

@@ -112,16 +112,18 @@ def d_noFlagOCCSolver(number_bands, nvband, ngpown, ncouls, inv_igp_index, wx_ar
 
 
 def d_reduce_achstemp(number_bands, inv_igp_index, ncouls, aqsmtemp, aqsntemp, I_eps_array,
-                      achstemp, ngpown, vcoul):
-    """reduce_achstemp over all bands (gppKerSeq.cpp:67-100); adds into achstemp[0]."""
+                      achstemp_re, achstemp_im, ngpown, vcoul):
+    """GPPComplex.h:308 (declared, never defined there): reduce_achstemp over
+    all bands (gppKerSeq.cpp:67-100); adds into achstemp_re[0] / achstemp_im[0]."""
     lib = capi.load()
     c128, f64, i32 = torch.complex128, torch.float64, torch.int32
-    st = _with_stream(lib.gpp_reduce_achstemp, number_bands,
+    st = _with_stream(lib.gpp_reduce_achstemp_split, number_bands,
                       _ptr(inv_igp_index, i32, "inv_igp_index", ngpown), ncouls,
                       _ptr(aqsmtemp, c128, "aqsmtemp", number_bands * ncouls),
                       _ptr(aqsntemp, c128, "aqsntemp", number_bands * ncouls),
                       _ptr(I_eps_array, c128, "I_eps_array", ngpown * ncouls),
-                      _ptr(achstemp, c128, "achstemp", 1), ngpown, _ptr(vcoul, f64, "vcoul", ncouls))
+                      _ptr(achstemp_re, f64, "achstemp_re", 1), _ptr(achstemp_im, f64, "achstemp_im", 1),
+                      ngpown, _ptr(vcoul, f64, "vcoul", ncouls))
     capi.check(st, "d_reduce_achstemp")
 
 
@@ -161,13 +163,17 @@ class DeviceInputs:
                    t(inp.inv_igp_index), t(inp.indinv) if with_indinv else None, t(wx), stride)
 
 
-def device_inputs(shape, seed: int = 20240607, device="cuda") -> DeviceInputs:
+def device_inputs(shape, seed: int = 20240607, device="cuda",
+                  rows: tuple[int, int] | None = None) -> DeviceInputs:
     """Seeded workload generated directly in device memory (same bits as
-    workload.make_inputs, without the host round trip)."""
+    workload.make_inputs, without the host round trip).  rows = (r0, r1):
+    only G' rows [r0, r1) of the G'-indexed arrays are made and held (one
+    rank's share of a row-sharded state); ngpown is then r1 - r0."""
     from . import workload
-    t = workload.make_inputs_device(shape, seed, device)
+    t = workload.make_inputs_device(shape, seed, device, rows=rows)
     stride = 0 if t["wx_array"].shape[0] == 1 and shape.number_bands != 1 else shape.nw
-    return DeviceInputs(shape.number_bands, shape.nvband, shape.ncouls, shape.ngpown, shape.nw,
+    ng = shape.ngpown if rows is None else rows[1] - rows[0]
+    return DeviceInputs(shape.number_bands, shape.nvband, shape.ncouls, ng, shape.nw,
                         t["aqsmtemp"], t["aqsntemp"], t["I_eps_array"], t["wtilde_array"],
                         t["vcoul"], t["inv_igp_index"], t["indinv"], t["wx_array"], stride)
 
@@ -296,6 +302,17 @@ class HostContext:
             o.achstemp = res["achstemp"].ctypes.data
         capi.check(self._lib.gpp_sigma_host(self.handle, C.byref(p), C.byref(o)), "gpp_sigma_host")
         return res
+
+    def last_trace(self) -> dict:
+        """Timeline of the last sigma call (ms after its first copy): when the
+        band arrays and each row piece landed, and when the kernels reached
+        each piece."""
+        n = C.c_int()
+        buf = (C.c_float * (1 + 2 * 16))()
+        capi.check(self._lib.gpp_context_last_trace(self.handle, buf, len(buf), C.byref(n)),
+                   "gpp_context_last_trace")
+        v = [round(buf[i], 2) for i in range(n.value)]
+        return {"bands": v[0], "piece_landed": v[1::2], "piece_started": v[2::2]}
 
     def last_timing(self) -> dict:
         """Device-side milliseconds of the last sigma call: H2D copies,

@@ -244,8 +244,11 @@ def torch_bitxor(a, b):
     return torch.bitwise_xor(a, b)
 
 
-def uniform_t(seed: int, stream: int, n: int, lo: float, hi: float, device, out=None):
-    """Device twin of uniform(): the same n doubles, as a float64 tensor."""
+def uniform_t(seed: int, stream: int, n: int, lo: float, hi: float, device, out=None,
+              offset: int = 0):
+    """Device twin of uniform(): the same doubles, as a float64 tensor --
+    values offset .. offset + n - 1 of the stream (the generator is
+    counter-based, so any range comes out with the bits it has in the whole)."""
     import torch
     if out is None:
         out = torch.empty(n, dtype=torch.float64, device=device)
@@ -255,36 +258,47 @@ def uniform_t(seed: int, stream: int, n: int, lo: float, hi: float, device, out=
     chunk = 1 << 26
     for s in range(0, n, chunk):
         e = min(n, s + chunk)
-        ctr = torch.arange(s + 1, e + 1, dtype=torch.int64, device=device)
+        ctr = torch.arange(offset + s + 1, offset + e + 1, dtype=torch.int64, device=device)
         z = _mix_t(ctr * golden + key)
         u = _lsr(z, 11).to(torch.float64) * (1.0 / 9007199254740992.0)
         out[s:e] = u * scale + lo
     return out
 
 
-def _complex_t(seed, s_re, s_im, rows, cols, lo_re, hi_re, lo_im, hi_im, device):
+def _complex_t(seed, s_re, s_im, rows, cols, lo_re, hi_re, lo_im, hi_im, device, row0=0):
+    """Rows row0 .. row0 + rows - 1 of a [*][cols] complex array."""
     import torch
     z = torch.empty((rows, cols), dtype=torch.complex128, device=device)
     v = torch.view_as_real(z).view(rows * cols, 2)
     n = rows * cols
-    v[:, 0] = uniform_t(seed, s_re, n, lo_re, hi_re, device)
-    v[:, 1] = uniform_t(seed, s_im, n, lo_im, hi_im, device)
+    v[:, 0] = uniform_t(seed, s_re, n, lo_re, hi_re, device, offset=row0 * cols)
+    v[:, 1] = uniform_t(seed, s_im, n, lo_im, hi_im, device, offset=row0 * cols)
     return z
 
 
-def make_inputs_device(shape: Shape, seed: int = 20240607, device="cuda") -> dict:
+def make_inputs_device(shape: Shape, seed: int = 20240607, device="cuda",
+                       rows: tuple[int, int] | None = None) -> dict:
     """make_inputs() generated directly on `device` (torch tensors, same bits):
     keys aqsmtemp, aqsntemp, I_eps_array, wtilde_array, vcoul,
-    inv_igp_index, indinv, wx_array."""
+    inv_igp_index, indinv, wx_array.  With rows = (r0, r1) only the G' rows
+    [r0, r1) of I_eps_array, wtilde_array and inv_igp_index are made (the
+    share of one rank of a row-sharded state), with the bits those rows have
+    in the whole state."""
     import torch
     nb, nc, ng, nw = shape.number_bands, shape.ncouls, shape.ngpown, shape.nw
     if not (0 <= shape.nvband <= nb and nc > 0 and 0 <= ng <= nc and nw > 0):
         raise ValueError(f"bad shape {shape}")
+    r0, r1 = (0, ng) if rows is None else rows
+    if not 0 <= r0 <= r1 <= ng:
+        raise ValueError(f"bad row range {rows} for ngpown {ng}")
+    nr = r1 - r0
     out = {
         "aqsmtemp": _complex_t(seed, _S_AQSM_RE, _S_AQSM_IM, nb, nc, -0.5, 0.5, -0.5, 0.5, device),
         "aqsntemp": _complex_t(seed, _S_AQSN_RE, _S_AQSN_IM, nb, nc, -0.5, 0.5, -0.5, 0.5, device),
-        "I_eps_array": _complex_t(seed, _S_IEPS_RE, _S_IEPS_IM, ng, nc, -0.5, 0.5, -0.5, 0.5, device),
-        "wtilde_array": _complex_t(seed, _S_WT_RE, _S_WT_IM, ng, nc, 0.5, 2.0, -0.05, 0.05, device),
+        "I_eps_array": _complex_t(seed, _S_IEPS_RE, _S_IEPS_IM, nr, nc, -0.5, 0.5, -0.5, 0.5,
+                                  device, row0=r0),
+        "wtilde_array": _complex_t(seed, _S_WT_RE, _S_WT_IM, nr, nc, 0.5, 2.0, -0.05, 0.05,
+                                   device, row0=r0),
         "vcoul": uniform_t(seed, _S_VCOUL, nc, 0.1, 1.0, device),
     }
     keys = uniform_t(seed, _S_IGP, nc, 0.0, 1.0, device)
@@ -292,16 +306,16 @@ def make_inputs_device(shape: Shape, seed: int = 20240607, device="cuda") -> dic
     if shape.igp_overflow:
         k = min(shape.igp_overflow, ng)
         igp[ng - k:] = nc + torch.arange(k, dtype=torch.int32, device=device)
-    out["inv_igp_index"] = igp.contiguous()
+    out["inv_igp_index"] = igp[r0:r1].contiguous()
     wx = torch.from_numpy(make_wx(shape, seed)).to(device)
-    if shape.near_pole > 0.0 and ng > 0:
-        n = ng * nc
-        sel = uniform_t(seed, _S_POLE_SEL, n, 0.0, 1.0, device) < shape.near_pole
+    if shape.near_pole > 0.0 and nr > 0:
+        n, at = nr * nc, r0 * nc  # this range's elements of the [ng][nc] streams
+        sel = uniform_t(seed, _S_POLE_SEL, n, 0.0, 1.0, device, offset=at) < shape.near_pole
         idx = torch.nonzero(sel).flatten()
-        band = torch.clamp((uniform_t(seed, _S_POLE_BAND, n, 0.0, 1.0, device)[idx] * nb).to(torch.int64), max=nb - 1)
-        iwk = torch.clamp((uniform_t(seed, _S_POLE_IW, n, 0.0, 1.0, device)[idx] * nw).to(torch.int64), max=nw - 1)
-        dre = uniform_t(seed, _S_POLE_DRE, n, -7e-5, 7e-5, device)[idx]
-        dim = uniform_t(seed, _S_POLE_DIM, n, -7e-5, 7e-5, device)[idx]
+        band = torch.clamp((uniform_t(seed, _S_POLE_BAND, n, 0.0, 1.0, device, offset=at)[idx] * nb).to(torch.int64), max=nb - 1)
+        iwk = torch.clamp((uniform_t(seed, _S_POLE_IW, n, 0.0, 1.0, device, offset=at)[idx] * nw).to(torch.int64), max=nw - 1)
+        dre = uniform_t(seed, _S_POLE_DRE, n, -7e-5, 7e-5, device, offset=at)[idx]
+        dim = uniform_t(seed, _S_POLE_DIM, n, -7e-5, 7e-5, device, offset=at)[idx]
         flat = torch.view_as_real(out["wtilde_array"]).view(-1, 2)
         flat[idx, 0] = wx[band, iwk] + dre
         flat[idx, 1] = dim

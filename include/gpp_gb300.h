@@ -116,6 +116,13 @@ gpp_status gpp_reduce_achstemp(int number_bands, const int *inv_igp_index, int n
                                const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
                                const gpp_complex *I_eps_array, gpp_complex *achstemp,
                                int ngpown, const double *vcoul);
+/* The same static term with the reference's split destination: d_reduce_achstemp
+ * (GPPComplex.h:308) takes double *achstemp_re, double *achstemp_im; the sum is
+ * ADDED into achstemp_re[0] / achstemp_im[0]. */
+gpp_status gpp_reduce_achstemp_split(int number_bands, const int *inv_igp_index, int ncouls,
+                                     const gpp_complex *aqsmtemp, const gpp_complex *aqsntemp,
+                                     const gpp_complex *I_eps_array, double *achstemp_re,
+                                     double *achstemp_im, int ngpown, const double *vcoul);
 
 /* Stream used by the drop-in entry points above (per host thread). */
 gpp_status gpp_set_stream(gpp_stream_t stream);
@@ -199,6 +206,14 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
  * device-to-host copy (milliseconds; any pointer may be NULL). */
 gpp_status gpp_context_last_timing(gpp_context *ctx, float *h2d_ms, float *compute_ms,
                                    float *d2h_ms);
+/* The last call's timeline, milliseconds after its first copy began:
+ * ms[0] = band arrays landed; then per row piece k, ms[1 + 2k] = the piece's
+ * rows landed and ms[2 + 2k] = the kernels' stream reached the piece (a
+ * piece whose start lies well after its landing was waiting on compute; the
+ * reverse means compute waited on the copy).  *count receives 1 + 2 x pieces;
+ * with capacity below it, only *count is set and GPP_ERR_INVALID_ARGUMENT
+ * is returned. */
+gpp_status gpp_context_last_trace(gpp_context *ctx, float *ms, int capacity, int *count);
 
 /* No counterpart in the reference.  gpp_sigma for callers that cannot
  * allocate device memory -- applications that have handed the GPU's memory

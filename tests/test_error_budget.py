@@ -1,0 +1,209 @@
+"""Error budget of the mixed-precision unoccupied term, step by step, on the CPU.
+
+The kernel's float-float term (gpp_tiles_mixed.cuh, mixed_column) is restated
+here operation for operation in C (float arithmetic with fmaf, no
+contraction) and evaluated on terms drawn like the benchmark's production
+shape: aqsn, I_eps ~ U(-0.5, 0.5), Re(wtilde) ~ U(0.5, 2), Im(wtilde) ~
+U(-0.05, 0.05), wx = 10 + (iw + 1) - e_n1, e_n1 ~ U(0, 20); terms within
+1e-3 |wx| of the pole are the FP64 path's and are left out.  Against a
+long-double evaluation of the same FP64 inputs it measures, per variant, the
+relative error of the sum of all terms (accumulated in long double, so only
+the per-term error shows), the RMS per-term relative error and the mean
+signed per-term error (a sign preference, which long sums amplify).
+
+Variants: the shipped form (Re(wdiff) by the exact coarse/fine subtraction
+where |Re(wdiff)| >= 0.5, by TwoSum elsewhere; the reciprocal folded into
+the products); the earlier TwoSum-everywhere form; the exact subtraction
+everywhere and at other radii; and the shipped form with one step at a time
+done in plain FP32 (its low part dropped).  The benchmark's bound is 1e-8
+per component and the kernels deliver ~1e-12; a step may leave float-float
+only if doing so keeps the sum within 1e-10.  None does: every FP32 step
+puts ~1e-8 to 1e-7 into the sum, because with random-sign terms the
+relative error of the sum is the per-term relative error itself.  The exact
+subtraction everywhere costs a factor ~25 on the sum (its ~2^-43 absolute
+error weighs on the large small-Re(wdiff) terms); from radius 0.25 on it
+costs nothing measurable.
+
+    python tests/test_error_budget.py [terms]   # prints the table
+"""
+import os
+import shutil
+import subprocess
+import sys
+
+import pytest
+
+HARNESS = r"""
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+
+typedef struct { float h, l; } df;
+
+static df two_sum(float a, float b) { float s = a + b, bb = s - a; return (df){s, (a - (s - bb)) + (b - bb)}; }
+static df df_add(df a, df b) { df s = two_sum(a.h, b.h); s.l = s.l + (a.l + b.l); return s; }
+static df df_sub(df a, df b) {  /* two_diff2 of gpp_df2.cuh */
+    float s = a.h - b.h, bb = s - a.h; df r = {s, (a.h - (s - bb)) - (b.h + bb)};
+    r.l = r.l + (a.l - b.l); return r;
+}
+static df df_mul(df a, df b) {
+    float p = a.h * b.h, e = fmaf(a.h, b.h, -p); e = fmaf(a.h, b.l, e); e = fmaf(a.l, b.h, e);
+    return (df){p, e};
+}
+static df df_sqr(df a) { float p = a.h * a.h, e = fmaf(a.h, a.h, -p); e = fmaf(a.h + a.h, a.l, e); return (df){p, e}; }
+static df df_norm(df a) { float s = a.h + a.l; return (df){s, a.l - (s - a.h)}; }
+static df split(double x) { float h = (float)x; return (df){h, (float)(x - (double)h)}; }
+static int coarse_fine(df *x) {
+    if (!(fabsf(x->h) < 16.f)) return 0;
+    float c = (x->h + 48.f) - 48.f; *x = (df){c, (x->h - c) + x->l}; return 1;
+}
+static df f32(df a) { return (df){a.h, 0.f}; }  /* drop the low part */
+
+static unsigned long long st = 88172645463325252ull;
+static double uni(void) {  /* SplitMix64 */
+    unsigned long long z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull; z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31; return (z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+enum { V_SHIPPED, V_TWOSUM, V_EXACT, V_H025, V_H1, V_A, V_AWTI, V_WTI2, V_WDIFF, V_D, V_RCP1, V_RCP, V_NUM, V_PROD, NV };
+static const char *names[NV] = {
+    "shipped: exact where |Re(wdiff)| >= 0.5", "TwoSum Re(wdiff), separate reciprocal",
+    "exact Re(wdiff) everywhere", "exact where |Re(wdiff)| >= 0.25",
+    "exact where |Re(wdiff)| >= 1",
+    "FP32: A = aqsn Q", "FP32: A Im(wtilde)", "FP32: Im(wtilde)^2", "FP32: Re(wdiff)",
+    "FP32: |wdiff|^2", "first-order reciprocal", "FP32: reciprocal", "FP32: numerator sums",
+    "FP32: products by 1/|wdiff|^2"};
+
+/* One term in float-float, variant v; returns re + i im as long doubles. */
+static void term(int v, df ar, df ai, df wtr, df wti, df qr, df qi, df wx, long double *re,
+                 long double *im) {
+    df wti2 = df_mul(wti, wti);
+    if (v == V_WTI2) wti2 = f32(wti2);
+    df Ar = df_sub(df_mul(ar, qr), df_mul(ai, qi)), Ai = df_add(df_mul(ar, qi), df_mul(ai, qr));
+    if (v == V_A) { Ar = f32(Ar); Ai = f32(Ai); }
+    df Ai_wti = df_mul(Ai, wti), Ar_wti = df_mul(Ar, wti);
+    if (v == V_AWTI) { Ai_wti = f32(Ai_wti); Ar_wti = f32(Ar_wti); }
+    df wr;
+    /* The kernel's chunk test (value buckets) is coarser than this per-term
+       one: it only ever sends more terms to the general form. */
+    const float far = v == V_H025 ? 0.25f : v == V_H1 ? 1.0f : v == V_EXACT ? 0.f : 0.5f;
+    if (v == V_TWOSUM || (far > 0.f && !(fabsf(wx.h - wtr.h) >= far))) {
+        wr = df_norm(df_sub(wx, wtr));
+    } else {
+        df x = wx, t = wtr;
+        if (!coarse_fine(&x) || !coarse_fine(&t)) { wr = df_norm(df_sub(wx, wtr)); }
+        else { wr = df_norm((df){x.h - t.h, x.l - t.l}); }
+    }
+    if (v == V_WDIFF) wr = (df){(float)((double)wx.h + wx.l - ((double)wtr.h + wtr.l)), 0.f};
+    df d = df_add(df_sqr(wr), wti2);
+    if (v == V_D) d = f32(d);
+    float r0 = 1.0f / d.h, e = fmaf(-d.h, r0, 1.0f); e = fmaf(-d.l, r0, e);
+    float c = (v == V_RCP1) ? e : fmaf(e, e, e);
+    if (v == V_RCP) c = 0.f;
+    df nre = df_sub(df_mul(Ar, wr), Ai_wti), nim = df_add(df_mul(Ai, wr), Ar_wti);
+    if (v == V_NUM) { nre = (df){Ar.h * wr.h - Ai_wti.h, 0.f}; nim = (df){Ai.h * wr.h + Ar_wti.h, 0.f}; }
+    df tre, tim;
+    if (v == V_TWOSUM) {  /* df_mul by the df reciprocal (r0, r0 c) */
+        df r = {r0, r0 * c}; tre = df_mul(nre, r); tim = df_mul(nim, r);
+    } else {
+        float p = nre.h * r0, q = fmaf(nre.h, r0, -p); q = fmaf(p, c, q); q = fmaf(nre.l, r0, q); tre = (df){p, q};
+        p = nim.h * r0; q = fmaf(nim.h, r0, -p); q = fmaf(p, c, q); q = fmaf(nim.l, r0, q); tim = (df){p, q};
+    }
+    if (v == V_PROD) { tre = (df){nre.h * r0, 0.f}; tim = (df){nim.h * r0, 0.f}; }
+    *re = (long double)tre.h + tre.l;
+    *im = (long double)tim.h + tim.l;
+}
+
+int main(int argc, char **argv) {
+    const long n = argc > 1 ? atol(argv[1]) : 2000000;
+    long double sref_re = 0, sref_im = 0, s_re[NV] = {0}, s_im[NV] = {0};
+    double rms[NV] = {0}, bias[NV] = {0};
+    long used = 0;
+    for (long i = 0; i < n; ++i) {
+        const double a_re = uni() - 0.5, a_im = uni() - 0.5, e_re = uni() - 0.5, e_im = uni() - 0.5;
+        const double w_re = 0.5 + 1.5 * uni(), w_im = -0.05 + 0.1 * uni();
+        const double wxv = 10.0 + (double)(1 + (int)(uni() * 3)) - 20.0 * uni();
+        const double q_re = w_re * e_re - w_im * e_im, q_im = w_re * e_im + w_im * e_re;
+        const double wr64 = wxv - w_re;
+        if (wr64 * wr64 + w_im * w_im < 1e-6 * wxv * wxv) continue;  /* FP64 pole path */
+        ++used;
+        /* Reference: long double from the same FP64 inputs (Q as the kernel's prep pass forms it). */
+        const long double Ar = (long double)a_re * q_re - (long double)a_im * q_im;
+        const long double Ai = (long double)a_re * q_im + (long double)a_im * q_re;
+        const long double wr = (long double)wxv - w_re, wi = w_im;
+        const long double den = wr * wr + wi * wi;
+        const long double tr = (Ar * wr - Ai * wi) / den, ti = (Ai * wr + Ar * wi) / den;
+        sref_re += tr; sref_im += ti;
+        const df ar = split(a_re), ai = split(a_im), wtr = split(w_re), wti = split(w_im);
+        const df qr = split(q_re), qi = split(q_im), wx = split(wxv);
+        const long double mag = sqrtl(tr * tr + ti * ti);
+        for (int v = 0; v < NV; ++v) {
+            long double gr, gi;
+            term(v, ar, ai, wtr, wti, qr, qi, wx, &gr, &gi);
+            s_re[v] += gr; s_im[v] += gi;
+            const double er = (double)((gr - tr) / mag), ei = (double)((gi - ti) / mag);
+            rms[v] += er * er + ei * ei;
+            bias[v] += er + ei;
+        }
+    }
+    printf("%ld terms (%ld outside the pole distance)\n", n, used);
+    printf("%-46s %12s %12s %12s\n", "variant", "sum rel err", "term RMS", "mean signed");
+    for (int v = 0; v < NV; ++v) {
+        const double er = (double)fabsl((s_re[v] - sref_re) / sref_re);
+        const double ei = (double)fabsl((s_im[v] - sref_im) / sref_im);
+        printf("%-46s %12.3e %12.3e %12.3e\n", names[v], er > ei ? er : ei,
+               sqrt(rms[v] / (2.0 * used)), bias[v] / (2.0 * used));
+    }
+    return 0;
+}
+"""
+
+
+def _build(tmp_path):
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "error_budget.c"
+    src.write_text(HARNESS)
+    exe = tmp_path / "error_budget"
+    r = subprocess.run([cc, "-O2", "-ffp-contract=off", str(src), "-o", str(exe), "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def run_table(tmp_path, terms: int) -> dict:
+    exe = _build(tmp_path)
+    out = subprocess.run([str(exe), str(terms)], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    rows = {}
+    for line in out.stdout.splitlines()[2:]:
+        name, vals = line[:46].strip(), line[46:].split()
+        rows[name] = [float(x) for x in vals]
+    return rows, out.stdout
+
+
+def test_no_step_of_the_term_can_leave_float_float(tmp_path):
+    rows, text = run_table(tmp_path, 1_000_000)
+    shipped = rows["shipped: exact where |Re(wdiff)| >= 0.5"]
+    twosum = rows["TwoSum Re(wdiff), separate reciprocal"]
+    everywhere = rows["exact Re(wdiff) everywhere"]
+    # The shipped form and the earlier one: per-term error ~2^-44, no bias,
+    # the same error on the sum.
+    for r in (shipped, twosum):
+        assert r[0] <= 1e-11 and r[1] <= 1e-13 and abs(r[2]) <= 1e-15, text
+    assert shipped[0] <= 2 * twosum[0], text
+    # Why the exact subtraction is confined to |Re(wdiff)| >= 0.5.
+    assert everywhere[0] > 5 * shipped[0], text
+    for name, r in rows.items():
+        if name.startswith("FP32:"):
+            # Each plain-FP32 step puts more than the 1e-10 target into the sum.
+            assert r[0] > 1e-10 or r[1] > 1e-10, (name, text)
+
+
+if __name__ == "__main__":
+    import pathlib
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        print(run_table(pathlib.Path(d), int(sys.argv[1]) if len(sys.argv) > 1 else 20_000_000)[1])

@@ -106,12 +106,20 @@ def test_reference_entry_points_accumulate_like_the_reference():
     im0 = torch.zeros(3, dtype=torch.float64, device="cuda")
     o.gppKernelGPU(d.wtilde_array, d.aqsntemp, d.aqsmtemp, d.I_eps_array, s.ncouls, s.ngpown,
                    s.number_bands, d.wx_array, re0, im0, d.vcoul, 0, 3, d.indinv, d.inv_igp_index)
-    achs = torch.zeros(1, dtype=torch.complex128, device="cuda")
+    achs_re = torch.zeros(1, dtype=torch.float64, device="cuda")
+    achs_im = torch.zeros(1, dtype=torch.float64, device="cuda")
     o.d_reduce_achstemp(s.number_bands, d.inv_igp_index, s.ncouls, d.aqsmtemp, d.aqsntemp,
-                        d.I_eps_array, achs, s.ngpown, d.vcoul)
+                        d.I_eps_array, achs_re, achs_im, s.ngpown, d.vcoul)
+    # The C ABI's complex-destination form gives the same bits.
+    achs = torch.zeros(1, dtype=torch.complex128, device="cuda")
+    capi.check(capi.load().gpp_reduce_achstemp(
+        s.number_bands, d.inv_igp_index.data_ptr(), s.ncouls, d.aqsmtemp.data_ptr(),
+        d.aqsntemp.data_ptr(), d.I_eps_array.data_ptr(), achs.data_ptr(), s.ngpown,
+        d.vcoul.data_ptr()), "gpp_reduce_achstemp")
     o.wait()
     assert rel_err((re0 + 1j * im0).cpu().numpy(), want0["achtemp"]) <= FP64_TOL
-    assert rel_err(achs.cpu().numpy(), want["achstemp"]) <= FP64_TOL
+    assert rel_err((achs_re + 1j * achs_im).cpu().numpy(), want["achstemp"]) <= FP64_TOL
+    assert torch.equal(torch.view_as_real(achs)[0], torch.stack([achs_re[0], achs_im[0]]))
 
 
 def test_bit_reproducible_run_to_run():

@@ -52,6 +52,23 @@ def _worker(rank, world, port, mode, out):
             total = [gd.sum_in_rank_order(part[k], dist) for k in ("achtemp", "asxtemp", "achstemp")]
             if rank == 0:
                 out[0] = total
+        elif mode == "rows_bench":
+            # bench.py --shard rows: each rank generates and holds only its
+            # rows (gd.rank_rows_inputs, here on the CPU), sums them (the
+            # oracle standing in for the GPU call) and the partials are added
+            # on rank 0 in rank order.
+            shape = W.Shape(8, 2, 300, 11, 3, near_pole=0.03)
+            d, (r0, r1) = gd.rank_rows_inputs(shape, 6, rank, world, device="cpu")
+            assert d.ngpown == r1 - r0 == d.I_eps_array.shape[0] == d.wtilde_array.shape[0]
+            inp = W.Inputs(W.Shape(8, 2, 300, r1 - r0, 3, near_pole=0.03), 6,
+                           d.aqsmtemp.numpy(), d.aqsntemp.numpy(), d.I_eps_array.numpy(),
+                           d.wtilde_array.numpy(), d.vcoul.numpy(), d.inv_igp_index.numpy(),
+                           d.indinv.numpy(), d.wx_array.numpy())
+            part = oracle_py.run(inp)
+            total = [gd.sum_in_rank_order(part[k], dist) for k in ("achtemp", "asxtemp", "achstemp")]
+            if rank == 0:
+                out[0] = total
+            out[("rows", rank)] = (r0, r1)
         elif mode == "rank_fails":
             if rank == 1:
                 raise RuntimeError("rank 1 fails before the collective")
@@ -119,3 +136,19 @@ def test_failing_rank_surfaces_on_its_peer():
     out, codes = _run("rank_fails")
     assert codes[1] != 0
     assert out[0] != "no error"
+
+
+def test_bench_row_sharding_holds_only_its_rows_and_adds_up():
+    """The code path of bench.py --shard rows (gppsigma.dist.rank_rows_inputs
+    + sum_in_rank_order), world size 2 over gloo: each rank holds only its
+    G' rows, and the rank-ordered sum of the ranks' partials equals the
+    oracle's sums over the whole state."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    from gppsigma import workload as W
+    out, codes = _run("rows_bench")
+    assert codes == [0, 0]
+    assert out[("rows", 0)] == (0, 6) and out[("rows", 1)] == (6, 11)
+    want = oracle_py.run(W.make_inputs(W.Shape(8, 2, 300, 11, 3, near_pole=0.03), 6))
+    for got, key in zip(out[0], ("achtemp", "asxtemp", "achstemp")):
+        np.testing.assert_allclose(got, want[key], rtol=1e-12)
