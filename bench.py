@@ -51,14 +51,13 @@ FLOPS_PER_TRIPLE = 12.0
 
 def mixed_fp32_ops_per_term(nwc: int) -> float:
     """FP32 operations the mixed kernel issues per unoccupied term, counted
-    from its column routine (the exact-subtraction form every chunk takes
-    when Re(wtilde) and wx lie below 16): per ig column a thread issues 44
-    packed instructions shared by its frequencies (A = aqsn*Q, A*Im(wtilde),
-    Im(wtilde)^2) and 68 per frequency (Re(wdiff) 2 + renormalisation 3,
+    from its column routine: per ig column a thread issues 44 packed
+    instructions shared by its frequencies (A = aqsn*Q, A*Im(wtilde),
+    Im(wtilde)^2) and 74 per frequency (Re(wdiff) 8 + renormalisation 3,
     |wdiff|^2 12, reciprocal 3, the two numerators 24, the two products by
     the reciprocal 8, the two accumulations 16), each packed instruction
     doing one FP32 operation for each of the tile's two rows."""
-    return (44.0 + 68.0 * nwc) / nwc
+    return (44.0 + 74.0 * nwc) / nwc
 
 
 class ClockSampler:
@@ -302,24 +301,24 @@ def run_batched(args, ws, rank, local) -> int:
     devs = [ops.device_inputs(s, gdist.state_seed(SEED, rank) + i) for i, s in enumerate(shapes)]
     terms = sum(s.terms for s in shapes)
 
-    def plan(precision):
-        probs = (capi.GppProblem * len(devs))()
-        outs = (capi.GppOutputs * len(devs))()
+    def plan(precision, states):
+        probs = (capi.GppProblem * len(states))()
+        outs = (capi.GppOutputs * len(states))()
         res = []
-        for i, d in enumerate(devs):
+        for i, d in enumerate(states):
             probs[i] = ops.problem_struct(d, precision, "complex_seq", 1.0)
             a = torch.empty(3, dtype=torch.complex128, device="cuda")
             x = torch.empty(3, dtype=torch.complex128, device="cuda")
             outs[i].achtemp, outs[i].asxtemp = a.data_ptr(), x.data_ptr()
             res.append((a, x))
         h = C.c_void_p()
-        capi.check(lib.gpp_batch_create(C.byref(h), probs, outs, len(devs)), "gpp_batch_create")
+        capi.check(lib.gpp_batch_create(C.byref(h), probs, outs, len(states)), "gpp_batch_create")
         return h, res
 
     stream = torch.cuda.Stream()
 
-    def timed(precision, steps, warmup):
-        h, res = plan(precision)
+    def timed(precision, steps, warmup, states):
+        h, res = plan(precision, states)
         with torch.cuda.stream(stream):
             for _ in range(warmup):
                 capi.check(lib.gpp_batch_run(h, stream.cuda_stream), "gpp_batch_run")
@@ -338,7 +337,7 @@ def run_batched(args, ws, rank, local) -> int:
 
     clocks = ClockSampler(local)
     clocks.start()
-    res, ms, launches = timed("mixed", args.steps, args.warmup)
+    res, ms, launches = timed("mixed", args.steps, args.warmup, devs)
     clk = clocks.stop()
     line = {"metric": METRIC, "value": ws * terms / (ms * 1e-3), "unit": "terms/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -350,14 +349,26 @@ def run_batched(args, ws, rank, local) -> int:
                        "l2": "inputs larger than L2 (129 MB)"},
             "gpu_launches": int(launches), "clocks": clk}
     if args.fp64_steps > 0:
-        r64, ms64, _ = timed("fp64", args.fp64_steps, 1)
-        errs = []
-        for (a, x), (a64, x64) in zip(res, r64):
-            g = torch.view_as_real(a).flatten().cpu().numpy()
-            w = torch.view_as_real(a64).flatten().cpu().numpy()
-            errs.append(float(np.max(np.abs(g - w) / np.where(w == 0, 1.0, np.abs(w)))))
-        line["fp64"] = {"value": ws * terms / (ms64 * 1e-3), "ms_per_step": ms64,
-                        "max_rel_err_mixed_vs_fp64_achtemp": max(errs)}
+        # The FP64 leg over the first --fp64-states states (all by default;
+        # at full scale one FP64 step of all 64 takes minutes), labelled.
+        k = len(devs) if args.fp64_states <= 0 else min(args.fp64_states, len(devs))
+        sub = devs[:k]
+        sub_terms = sum(shapes[i].terms for i in range(k))
+        r64, ms64, _ = timed("fp64", args.fp64_steps, args.fp64_warmup, sub)
+        errs_a, errs_x = [], []
+
+        def rel(g, w):
+            g = torch.view_as_real(g).flatten().cpu().numpy()
+            w = torch.view_as_real(w).flatten().cpu().numpy()
+            return float(np.max(np.abs(g - w) / np.where(w == 0, 1.0, np.abs(w))))
+        for (a, x), (a64, x64) in zip(res[:k], r64):
+            errs_a.append(rel(a, a64))
+            errs_x.append(rel(x, x64))
+        line["fp64"] = {"value": ws * sub_terms / (ms64 * 1e-3), "ms_per_step": ms64,
+                        "states": k, "terms": sub_terms,
+                        "max_rel_err_mixed_vs_fp64": {"achtemp": max(errs_a),
+                                                      "asxtemp": max(errs_x)},
+                        "per_state_max_rel_err_achtemp": errs_a}
         line["mixed_speedup_vs_fp64"] = line["value"] / line["fp64"]["value"]
     if rank == 0:
         print(json.dumps(line))
@@ -374,6 +385,12 @@ def main() -> int:
                     choices=sorted(W.CONFIGS) + sorted(BATCHED))
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-warmup", type=int, default=1,
+                    help="untimed FP64-leg calls after the first (0 for the 32-frequency sweep)")
+    ap.add_argument("--fp64-states", type=int, default=0,
+                    help="batched workloads: time the FP64 leg on the first K states (0: all)")
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="end-to-end calls timed (0: max(5, steps // 2))")
     ap.add_argument("--ref-seconds", type=float, default=4.0,
                     help="CPU seconds per step of the reference arm's band sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -477,7 +494,7 @@ def main() -> int:
     fp64_leg = None
     mixed_vs_oracle = None
     if precision == "mixed":
-        r64, ms64, k64, _ = timed("fp64", args.fp64_steps, 1)
+        r64, ms64, k64, _ = timed("fp64", args.fp64_steps, args.fp64_warmup)
         a, b = res.achtemp.cpu().numpy(), r64.achtemp.cpu().numpy()
         x, y = res.asxtemp.cpu().numpy(), r64.asxtemp.cpu().numpy()
 
@@ -526,7 +543,8 @@ def main() -> int:
     d2h = 2 * shape.nw * 16
     e2e_times, e2e_parts = [], []
     with ops.HostContext() as ctx:
-        for i in range(2 + max(5, args.steps // 2)):
+        n_e2e = args.e2e_steps if args.e2e_steps > 0 else max(5, args.steps // 2)
+        for i in range(2 + n_e2e):
             barrier()
             t0 = time.perf_counter()
             ctx.sigma(arrays, shape, precision)

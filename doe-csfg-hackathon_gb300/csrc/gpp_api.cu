@@ -162,11 +162,11 @@ void tune_cache_save_locked() {
 }
 
 int mixed_variant_for(int dev, int nw) {
-    if (t_force_variant >= 0) return t_force_variant;
+    if (t_force_variant >= 0 && mixed_variant_valid(t_force_variant, nw)) return t_force_variant;
     std::lock_guard<std::mutex> lk(g_tune_mutex);
     tune_cache_load_locked();
     const int v = g_tuned[dev & 255][nwc_of(nw)];
-    return v ? v - 1 : mixed_default_variant();
+    return (v && mixed_variant_valid(v - 1, nw)) ? v - 1 : mixed_default_variant();
 }
 
 // Per host thread and device: a highest-priority side stream plus fork/join
@@ -260,7 +260,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const bool mixed = precision == GPP_PRECISION_MIXED && (has_noflag || has_flag);
 
     const TileShape fs = flag_shape(p);  // same tiling for the FP64 and the mixed occupied tile
-    const TileShape ns = mixed ? mixed_noflag_shape(p) : fp64_noflag_shape(p);
+    const int variant = mixed ? mixed_variant_for(dev, p.nw) : 0;
+    const TileShape ns = mixed ? mixed_noflag_shape(p, variant) : fp64_noflag_shape(p);
     const bool want_n1 = o.n1 && p.nw >= 3 && p.ng > 0;
     const bool gemm = has_noflag && gemm_path(p.wx_stride, nb1 - nb0);
     const long long rows_f = has_flag ? ceil_div(p.ng, fs.rg) : 0;
@@ -324,7 +325,6 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
             return st;
         }
     }
-    const int variant = mixed ? mixed_variant_for(dev, p.nw) : 0;
     for (int k = 0; k < pc.n && e == cudaSuccess; ++k) {
         RowTiles rt;
         rt.begin = pc.pair[k];
@@ -742,6 +742,16 @@ struct gpp_context {
 // the unoccupied-band kernel.
 constexpr int kHostPieceCuts[] = {1, 5, 16};
 
+// How gpp_sigma_host moves its inputs: 0 = copy engine (default), 1 = SM
+// pull kernel (GPP_HOST_PULL=sm).
+int host_pull_mode() {
+    static const int mode = [] {
+        const char *v = getenv("GPP_HOST_PULL");
+        return (v && strcmp(v, "sm") == 0) ? 1 : 0;
+    }();
+    return mode;
+}
+
 // The piece cuts in effect: GPP_HOST_PIECES="c1,c2,...,16" (increasing
 // sixteenths ending at 16, at most kMaxRowPieces of them) overrides the
 // default, for hosts whose links move rows at another speed.
@@ -849,7 +859,24 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     }
     char *d = static_cast<char *>(ctx->dev);
     ctx->timed = false;
+    // Transfers: copy engine by default; with GPP_HOST_PULL=sm the SMs pull
+    // every input the device can address (pinned host memory, 16-byte
+    // aligned) with a kernel on the copy stream, before the computation (the
+    // computation's blocks fill the SMs, so the pull gets no room beside it).
+    const bool sm_pull = host_pull_mode() == 1;
+    std::vector<const char *> src_dev(in.size(), nullptr);
+    if (sm_pull)
+        for (size_t k = 0; k < in.size(); ++k) {
+            void *dp = nullptr;
+            if (in[k].bytes && ((uintptr_t)in[k].src & 15) == 0 && (in[k].bytes & 15) == 0 &&
+                cudaHostGetDevicePointer(&dp, const_cast<void *>(in[k].src), 0) == cudaSuccess)
+                src_dev[k] = static_cast<const char *>(dp);
+            else
+                cudaGetLastError();  // not device-accessible: the copy engine moves it
+        }
     auto h2d = [&](int k, size_t from, size_t bytes) {
+        if (src_dev[k] && (from & 15) == 0 && (bytes & 15) == 0)
+            return launch_host_pull(d + in[k].off + from, src_dev[k] + from, bytes, ctx->copy);
         return cudaMemcpyAsync(d + in[k].off + from, static_cast<const char *>(in[k].src) + from,
                                bytes, cudaMemcpyHostToDevice, ctx->copy);
     };
@@ -864,7 +891,7 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     const int pairs = (int)((ng + 1) / 2);
     pieces.n = 0;
     pieces.pair[0] = 0;
-    for (int cut : host_piece_cuts()) {
+    for (int cut : (sm_pull ? std::vector<int>{16} : host_piece_cuts())) {
         const int b = (int)((long long)pairs * cut / 16);
         if (b > pieces.pair[pieces.n]) pieces.pair[++pieces.n] = b;
     }
@@ -961,6 +988,8 @@ const char *gpp_variant_name(int variant) { return mixed_variant_name(variant); 
 gpp_status gpp_set_variant(int nw, int variant) {
     if (nw <= 0 || variant < -1 || variant >= mixed_variant_count())
         return fail(GPP_ERR_INVALID_ARGUMENT, "bad nw or variant");
+    if (variant >= 0 && !mixed_variant_valid(variant, nw))
+        return fail(GPP_ERR_UNSUPPORTED, "variant %d is not compiled for %d frequencies", variant, nw);
     int dev = 0;
     GPP_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
     std::lock_guard<std::mutex> lk(g_tune_mutex);
@@ -1006,6 +1035,7 @@ gpp_status gpp_autotune(const gpp_problem *problem, int max_bands, gpp_stream_t 
     const bool timing = t_timing;
     t_timing = false;
     for (int v = 0; v < mixed_variant_count() && st == GPP_OK; ++v) {
+        if (!mixed_variant_valid(v, p.nw)) continue;
         t_force_variant = v;
         float vbest = 0.f;
         for (int rep = 0; rep < 3 && st == GPP_OK; ++rep) {

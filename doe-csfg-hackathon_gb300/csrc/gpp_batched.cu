@@ -258,7 +258,10 @@ gpp_status plan_batch(gpp_batch *b, const gpp_problem *problems, const gpp_outpu
     Problem p0{};
     p0.nw = nw;
     const TileShape fs = flag_shape(p0);
-    const TileShape ns = mixed ? mixed_noflag_shape(p0) : fp64_noflag_shape(p0);
+    // The persistent unoccupied-band kernel is compiled in the default
+    // variant's shape (4 bands x 2 rows).
+    const TileShape ns =
+        mixed ? mixed_noflag_shape(p0, mixed_default_variant()) : fp64_noflag_shape(p0);
 
     struct StateGeom {
         long long rows_f, rows_n, tiles_f, tiles_n, ach_seg, n1_seg;

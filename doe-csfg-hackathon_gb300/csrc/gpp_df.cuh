@@ -107,23 +107,6 @@ __host__ __device__ __forceinline__ df split(double x) {
 }
 __host__ __device__ __forceinline__ double to_double(df a) { return (double)a.h + (double)a.l; }
 
-// Coarse/fine form of a df value, for an exact subtraction of the main
-// parts: c = x.h rounded to a multiple of 2^-18, f = (x.h - c) + x.l with
-// |f| <= 2^-19 + |x.l| (< 2^-18).  The sum c + f equals x to within one
-// rounding of f (<= 2^-43).  Two values in this form with |c| <= 16 subtract exactly
-// in their coarse parts: c1 - c2 is a multiple of 2^-18 below 32 in
-// magnitude, at most 23 significant bits.  Rounding x.h to the grid is the
-// classic add-and-subtract of a constant (48 = 1.5 * 2^5: for |x.h| < 16 the
-// sum lies in [32, 64), whose ulp is 2^-18); x.h - c is exact (a multiple of
-// ulp(x.h) no larger than 2^-19).  For |x.h| >= 16, NaN or Inf the value is
-// left as it is and false is returned.
-constexpr float kCoarseBound = 16.f;
-__host__ __device__ __forceinline__ bool coarse_fine(df &x) {
-    if (!(fabsf(x.h) < kCoarseBound)) return false;
-    const float c = fsub(fadd(x.h, 48.f), 48.f);
-    x = {c, fadd(fsub(x.h, c), x.l)};
-    return true;
-}
 
 // Small integer k (|k| < 2^22) to float, exactly, without a conversion
 // instruction: 1.5 * 2^23 + k has k in its low mantissa bits.

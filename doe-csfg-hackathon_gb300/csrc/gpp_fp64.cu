@@ -8,6 +8,8 @@
 // bit-reproducible.
 #include <cstdio>
 
+#include <algorithm>
+
 #include "gpp_kernels.h"
 #include "gpp_tiles_fp64.cuh"
 
@@ -178,6 +180,30 @@ cudaError_t launch_reduce(const double2 *src, long long stride, int len, int nse
 // ---------------------------------------------------------------------------
 // FMA throughput probe: independent FMA chains, enough warps to fill the SMs.
 namespace {
+// Host-to-device transfer by the SMs: each thread streams 16-byte words
+// from host memory the device can address (pinned, mapped into the device's
+// address space) into device memory.  The alternative to a copy-engine
+// cudaMemcpyAsync for the host path (gpp_sigma_host); `bytes` is a multiple
+// of 16 and both pointers are 16-byte aligned (the caller checks).
+__global__ void __launch_bounds__(256) host_pull_kernel(uint4 *__restrict__ dst,
+                                                        const uint4 *__restrict__ src,
+                                                        size_t words) {
+    const size_t stride = (size_t)gridDim.x * 256;
+    size_t i = (size_t)blockIdx.x * 256 + threadIdx.x;
+    // Four independent 16-byte loads in flight per thread: host memory is a
+    // microsecond away.
+    for (; i + 3 * stride < words; i += 4 * stride) {
+        const uint4 a = src[i], b = src[i + stride], c = src[i + 2 * stride],
+                    d = src[i + 3 * stride];
+        dst[i] = a;
+        dst[i + stride] = b;
+        dst[i + 2 * stride] = c;
+        dst[i + 3 * stride] = d;
+    }
+    for (; i < words; i += stride) dst[i] = src[i];
+}
+
+
 template <typename T, int CHAINS>
 __global__ void __launch_bounds__(256) fma_probe_kernel(const T *in, T *out, int iters) {
     T a[CHAINS];
@@ -239,6 +265,20 @@ cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops) {
     e = time_probe<double>(blocks, 4096, fp64_tflops);
     if (e == cudaSuccess) e = time_probe<float>(blocks, 65536, fp32_tflops);
     return e;
+}
+
+cudaError_t launch_host_pull(void *dst, const void *src_dev, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return cudaSuccess;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t words = bytes / 16;
+    const size_t want = (words + 255) / 256;
+    const int grid = (int)std::min<size_t>(want, (size_t)std::max(1, sms) * 4);
+    host_pull_kernel<<<grid, 256, 0, s>>>(static_cast<uint4 *>(dst),
+                                           static_cast<const uint4 *>(src_dev), words);
+    count_launch();
+    return cudaGetLastError();
 }
 
 }  // namespace gpp

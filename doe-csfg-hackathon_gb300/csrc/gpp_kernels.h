@@ -57,12 +57,21 @@ struct ReduceOut {
 cudaError_t launch_reduce(const double2 *src, long long stride, int len, int nseg, ReduceOut out,
                           cudaStream_t s);
 
+// Host-to-device transfer by the SMs (host_pull_kernel): src_dev is the
+// device's address of device-accessible host memory; 16-byte aligned
+// pointers and a size that is a multiple of 16.
+cudaError_t launch_host_pull(void *dst, const void *src_dev, size_t bytes, cudaStream_t s);
+
 // FMA throughput probe (see gpp_probe_fma_peaks).
 cudaError_t probe_fma_peaks(double *fp64_tflops, double *fp32_tflops);
 
 // Mixed precision path (gpp_mixed.cu).
 size_t mixed_split_bytes(const Problem &p);
-TileShape mixed_noflag_shape(const Problem &p);
+// Tile shape of a variant of the unoccupied-band kernel (the default
+// variant's for one not compiled for this problem's frequency chunk), and
+// whether the variant is compiled for `nw` frequencies.
+TileShape mixed_noflag_shape(const Problem &p, int variant);
+bool mixed_variant_valid(int variant, int nw);
 // The split planes must have been written (launch_split) for the bands used:
 // [band_begin, band_end) for the unoccupied kernel, [0, nvband) for the
 // occupied one.

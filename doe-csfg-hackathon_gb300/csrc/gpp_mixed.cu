@@ -67,20 +67,17 @@ __global__ void __launch_bounds__(256) split_rows_kernel(Problem p, SplitPlanes 
             const double2 wt0 = __ldg(p.wt + r0 * nc + ig), wt1 = __ldg(p.wt + r1 * nc + ig);
             const double2 q0 = cmul(wt0, __ldg(p.ieps + r0 * nc + ig));
             const double2 q1 = cmul(wt1, __ldg(p.ieps + r1 * nc + ig));
-            df a0 = split_bits(wt0.x), a1 = split_bits(wt1.x);
+            const df a0 = split_bits(wt0.x), a1 = split_bits(wt1.x);
             const df b0 = split_bits(wt0.y), b1 = split_bits(wt1.y);
             const df c0 = split_bits(q0.x), c1 = split_bits(q1.x);
             const df d0 = split_bits(q0.y), d1 = split_bits(q1.y);
-            // Buckets of the nearest floats; then Re(wtilde) in coarse/fine
-            // form where it fits (kWideBit marks the chunk otherwise).
-            unsigned long long bits =
-                bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
-            if (!coarse_fine(a0) | !coarse_fine(a1)) bits |= kWideBit;
             float4 *o = s.rows + j * 4 * nc + ig;
             o[0] = make_float4(a0.h, a1.h, a0.l, a1.l);
             o[nc] = make_float4(b0.h, b1.h, b0.l, b1.l);
             o[2 * nc] = make_float4(c0.h, c1.h, c0.l, c1.l);
             o[3 * nc] = make_float4(d0.h, d1.h, d0.l, d1.l);
+            const unsigned long long bits =
+                bucket_bit(bucket_code(a0.h)) | bucket_bit(bucket_code(a1.h));
             const unsigned long long word = j * nmw + ig / kMaskCols;
             const unsigned act = __activemask();
             const unsigned grp = __match_any_sync(act, word);
@@ -104,8 +101,7 @@ __global__ void __launch_bounds__(256) split_bands_kernel(Problem p, SplitPlanes
     const int nwx = (b1 - b0) * p.nw;
     for (int i = blockIdx.x * 256 + threadIdx.x; i < nwx; i += gridDim.x * 256) {
         const int b = b0 + i / p.nw, iw = i % p.nw;
-        df x = split(__ldg(p.wx + (size_t)b * p.wx_stride + iw));
-        coarse_fine(x);  // (hi, lo) kept for |wx| >= 16
+        const df x = split(__ldg(p.wx + (size_t)b * p.wx_stride + iw));
         s.wx[(size_t)b * p.nw + iw] = make_float2(x.h, x.l);
     }
 }
@@ -131,30 +127,49 @@ mixed_noflag_kernel(Problem p, Partials part, SplitPlanes s, int band_begin, int
 constexpr int kGroup = 16;
 constexpr int kWarps = 4;
 
-// Compiled pipeline variants of the mixed kernel (the autotuner picks one).
-// `minb` is the __launch_bounds__ minimum of resident blocks per SM: 0 leaves
-// the register count to the compiler's default heuristic (a minimum of 1
-// would let it take up to 255), 5 caps it at 96 registers.
+// Compiled variants of the mixed kernel (the autotuner picks one): the tile
+// shape -- `warps` warps per block, each owning `rnw` bands of the block's
+// row pair, so warps x rnw bands x 2 rows per block -- and the shared-memory
+// pipeline (chunk width, stage count, recycling).  `minb` is the
+// __launch_bounds__ minimum of resident blocks per SM: 0 leaves the register
+// count to the compiler's default heuristic (a minimum of 1 would let it
+// take up to 255), 5 caps it at 96 registers.  The shape sets the block
+// partials' layout (and so the order of the final sums): variants of one
+// shape give identical bits, other shapes agree to rounding.
 struct MixedVariant {
-    int kc, stages, sync, minb;
+    int kc, stages, sync, minb, warps, rnw;
     const char *name;
 };
 constexpr MixedVariant kMixedVariants[] = {
-    {128, 2, kSyncBlock, 0, "block-sync, 2 x 128 columns"},
-    {128, 3, kSyncBlock, 0, "block-sync, 3 x 128 columns"},
-    {128, 2, kSyncRing, 0, "mbarrier ring, 2 x 128 columns"},
-    {64, 4, kSyncRing, 0, "mbarrier ring, 4 x 64 columns"},
-    {128, 2, kSyncBlock, 5, "block-sync, 2 x 128 columns, 5 blocks/SM"},
-    {128, 3, kSyncRing, 0, "mbarrier ring, 3 x 128 columns"},
-    {192, 2, kSyncBlock, 0, "block-sync, 2 x 192 columns"},
-    {256, 2, kSyncBlock, 0, "block-sync, 2 x 256 columns"},
+    {128, 2, kSyncBlock, 0, 4, 1, "4 bands x 2 rows, block-sync, 2 x 128 columns"},
+    {128, 3, kSyncBlock, 0, 4, 1, "4 bands x 2 rows, block-sync, 3 x 128 columns"},
+    {128, 2, kSyncRing, 0, 4, 1, "4 bands x 2 rows, mbarrier ring, 2 x 128 columns"},
+    {64, 4, kSyncRing, 0, 4, 1, "4 bands x 2 rows, mbarrier ring, 4 x 64 columns"},
+    {128, 2, kSyncBlock, 5, 4, 1, "4 bands x 2 rows, block-sync, 2 x 128 columns, 5 blocks/SM"},
+    {128, 3, kSyncRing, 0, 4, 1, "4 bands x 2 rows, mbarrier ring, 3 x 128 columns"},
+    {192, 2, kSyncBlock, 0, 4, 1, "4 bands x 2 rows, block-sync, 2 x 192 columns"},
+    {256, 2, kSyncBlock, 0, 4, 1, "4 bands x 2 rows, block-sync, 2 x 256 columns"},
+    {192, 2, kSyncBlock, 0, 8, 1, "8 bands x 2 rows (8 warps), block-sync, 2 x 192 columns"},
+    {256, 2, kSyncBlock, 0, 8, 1, "8 bands x 2 rows (8 warps), block-sync, 2 x 256 columns"},
+    {192, 2, kSyncBlock, 3, 4, 2, "8 bands x 2 rows (2 bands per warp), block-sync, 2 x 192 columns"},
 };
 constexpr int kNumMixedVariants = sizeof(kMixedVariants) / sizeof(kMixedVariants[0]);
 
-template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC, int MINB = 0>
+// Frequency chunks compiled in every variant: 3 (the workloads' grids) and
+// 8 (large grids); chunks of 1, 2 and 4 frequencies have one kernel, of
+// the 4 bands x 2 rows shape.  Two bands per warp double the accumulators:
+// that shape is compiled for 3 frequencies only (8 would spill heavily).
+bool variant_compiled(int v, int nwc) {
+    if (v < 0 || v >= kNumMixedVariants) return false;
+    const MixedVariant &m = kMixedVariants[v];
+    if (nwc != 3 && nwc != 8) return m.warps == kWarps && m.rnw == 1;
+    return !(m.rnw == 2 && nwc > 4);
+}
+
+template <int RNW, int RG, int NWC, int KC, int NSTAGE, int SYNC, int MINB = 0, int NWARP = kWarps>
 cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s, int b0,
                            int b1, RowTiles rt, cudaStream_t st) {
-    constexpr int BN = kWarps * RNW;
+    constexpr int BN = NWARP * RNW;
     const int row_tiles = ceil_div(p.ng, RG), band_tiles = ceil_div(b1 - b0, BN);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
@@ -162,34 +177,43 @@ cudaError_t launch_mixed_t(const Problem &p, const Partials &part, const SplitPl
     // The 8-frequency tile holds 64 accumulator registers: keep it at three
     // resident blocks unless the variant asks for more.
     constexpr int kMinB = MINB ? MINB : (NWC > 4 ? 3 : 0);
-    auto kern = mixed_noflag_kernel<RNW, RG, NWC, kWarps, KC, NSTAGE, SYNC, kGroup, kMinB>;
+    auto kern = mixed_noflag_kernel<RNW, RG, NWC, NWARP, KC, NSTAGE, SYNC, kGroup, kMinB>;
     // Opt in to the full dynamic size (the default cap is 48 KB including
     // the kernel's static shared memory).
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)(r.end - r.begin) * band_tiles, ceil_div(p.nw, NWC));
-    kern<<<grid, kWarps * 32, smem, st>>>(p, part, s, b0, b1, r.begin, r.end - r.begin, row_tiles,
-                                          band_tiles);
+    kern<<<grid, NWARP * 32, smem, st>>>(p, part, s, b0, b1, r.begin, r.end - r.begin, row_tiles,
+                                         band_tiles);
     count_launch();
     return cudaGetLastError();
 }
 
-template <int RNW, int RG, int NWC>
+template <int RG, int NWC>
 cudaError_t launch_mixed_variant(int v, const Problem &p, const Partials &part,
                                  const SplitPlanes &s, int b0, int b1, RowTiles rt,
                                  cudaStream_t st) {
     switch (v) {
-        case 0: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
-        case 2: return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, rt, st);
-        case 3: return launch_mixed_t<RNW, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, rt, st);
+        case 0: return launch_mixed_t<1, RG, NWC, 128, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 2: return launch_mixed_t<1, RG, NWC, 128, 2, kSyncRing>(p, part, s, b0, b1, rt, st);
+        case 3: return launch_mixed_t<1, RG, NWC, 64, 4, kSyncRing>(p, part, s, b0, b1, rt, st);
         case 4:
-            return launch_mixed_t<RNW, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, rt, st);
-        case 5: return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncRing>(p, part, s, b0, b1, rt, st);
-        case 6: return launch_mixed_t<RNW, RG, NWC, 192, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
-        case 7: return launch_mixed_t<RNW, RG, NWC, 256, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
+            return launch_mixed_t<1, RG, NWC, 128, 2, kSyncBlock, 5>(p, part, s, b0, b1, rt, st);
+        case 5: return launch_mixed_t<1, RG, NWC, 128, 3, kSyncRing>(p, part, s, b0, b1, rt, st);
+        case 6: return launch_mixed_t<1, RG, NWC, 192, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 7: return launch_mixed_t<1, RG, NWC, 256, 2, kSyncBlock>(p, part, s, b0, b1, rt, st);
+        case 8:
+            return launch_mixed_t<1, RG, NWC, 192, 2, kSyncBlock, 0, 8>(p, part, s, b0, b1, rt, st);
+        case 9:
+            return launch_mixed_t<1, RG, NWC, 256, 2, kSyncBlock, 0, 8>(p, part, s, b0, b1, rt, st);
+        case 10:
+            if constexpr (NWC <= 4)
+                return launch_mixed_t<2, RG, NWC, 192, 2, kSyncBlock, 3>(p, part, s, b0, b1, rt, st);
+            else
+                return cudaErrorInvalidValue;
         default:
-            return launch_mixed_t<RNW, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
+            return launch_mixed_t<1, RG, NWC, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
     }
 }
 
@@ -201,10 +225,14 @@ static int nwc_for(int nw) { return nw <= 4 ? nw : 8; }
 // packed df2 arithmetic.
 static int mixed_rg(int) { return 2; }
 
-TileShape mixed_noflag_shape(const Problem &p) {
+TileShape mixed_noflag_shape(const Problem &p, int variant) {
     const int nwc = nwc_for(p.nw);
-    return TileShape{kWarps, mixed_rg(nwc), nwc, kWarps * 32};
+    const MixedVariant &v =
+        kMixedVariants[variant_compiled(variant, nwc) ? variant : mixed_default_variant()];
+    return TileShape{v.warps * v.rnw, mixed_rg(nwc), nwc, v.warps * 32};
 }
+
+bool mixed_variant_valid(int variant, int nw) { return variant_compiled(variant, nwc_for(nw)); }
 
 int mixed_variant_count() { return kNumMixedVariants; }
 const char *mixed_variant_name(int v) {
@@ -332,9 +360,9 @@ cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *sp
     switch (nwc_for(p.nw)) {
         case 1: return launch_mixed_t<1, 2, 1, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
         case 2: return launch_mixed_t<1, 2, 2, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
-        case 3: return launch_mixed_variant<1, 2, 3>(variant, p, part, s, b0, b1, rt, st);
+        case 3: return launch_mixed_variant<2, 3>(variant, p, part, s, b0, b1, rt, st);
         case 4: return launch_mixed_t<1, 2, 4, 128, 3, kSyncBlock>(p, part, s, b0, b1, rt, st);
-        default: return launch_mixed_variant<1, 2, 8>(variant, p, part, s, b0, b1, rt, st);
+        default: return launch_mixed_variant<2, 8>(variant, p, part, s, b0, b1, rt, st);
     }
 }
 

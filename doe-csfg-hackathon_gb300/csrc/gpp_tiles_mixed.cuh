@@ -17,29 +17,20 @@ namespace gpp {
 // float4 planes per pair, so that one 16-byte load yields both rows' values
 // as two aligned register pairs, the operands of the packed f32x2
 // instructions:
-//   rows[j][0][ig] = (wt.re main part of row 2j, of row 2j+1, low part of 2j, of 2j+1)
-//   rows[j][1][ig] = (hi, hi, lo, lo) of wt.im
+//   rows[j][0][ig] = (wt.re hi of row 2j, hi of row 2j+1, lo of 2j, lo of 2j+1)
+//   rows[j][1][ig] = the same for wt.im
 //   rows[j][2][ig], rows[j][3][ig] = the same for Q.re, Q.im (Q = wt*I_eps, FP64)
-// Re(wtilde) and wx are stored in coarse/fine form (coarse_fine, gpp_df.cuh:
-// main part on the 2^-18 grid) wherever |value| < 16, so that the kernels
-// form Re(wdiff) = wx - Re(wtilde) with one exact subtraction of the main
-// parts; a value outside that range keeps its (hi, lo) split.  Both forms
-// are df values (the sum of the two parts), so every other use is the same.
-// masks[j][k] has a bit for every value bucket (below) that Re(wtilde) of
-// rows 2j, 2j+1 takes in columns 64k .. 64k+63, and bit 63 (kWideBit) when
-// one of those values is in (hi, lo) form; written by the row split.  A warp
-// takes the exact subtraction, and skips the per-term pole test, for a chunk
-// none of whose buckets can hold a wtilde within kNearRadius (plus the pole
-// distance) of its wx values; otherwise, and for a chunk with kWideBit, the
-// general (TwoSum) form with the pole test.
+// masks[j][k] has a bit for every value bucket (below) that Re(wtilde) hi of
+// rows 2j, 2j+1 takes in columns 64k .. 64k+63, written by the row split.
+// A warp skips the per-term pole test for a chunk when none of the chunk's
+// buckets can hold a wtilde within the pole distance of its wx values.
 struct SplitPlanes {
     float4 *rows;                 // [ceil(ng/2)][4][nc]
     float4 *band;                 // [nb][nc]: aqsn.re hi, lo, .im hi, lo
-    float2 *wx;                   // [nb][nw]: wx main, low part (coarse/fine below 16)
+    float2 *wx;                   // [nb][nw]: wx hi, lo
     unsigned long long *masks;    // [ceil(ng/2)][ceil(nc/64)], zeroed before the split
 };
 constexpr int kMaskCols = 64;
-constexpr unsigned long long kWideBit = 1ull << 63;
 // Monotonic map of floats onto unsigned integers (integer order = float
 // order).
 __host__ __device__ __forceinline__ unsigned float_key(float f) {
@@ -48,25 +39,17 @@ __host__ __device__ __forceinline__ unsigned float_key(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 // Value bucket: the top 11 bits of the key (sign, exponent, two mantissa
-// bits, in value order), hashed onto one of 63 mask bits (bit 63 is
-// kWideBit).  Shared bits only cost a needless test, never a missed one.
+// bits, in value order), hashed onto one of 64 mask bits.  Shared bits only
+// cost a needless test, never a missed one.
 __host__ __device__ __forceinline__ unsigned bucket_code(float f) { return float_key(f) >> 21; }
 __host__ __device__ __forceinline__ unsigned long long bucket_bit(unsigned code) {
-    return 1ull << ((code ^ (code >> 6)) % 63u);
+    return 1ull << ((code ^ (code >> 6)) & 63);
 }
-// Terms with |Re(wdiff)| below kNearRadius take the general form of
-// Re(wdiff): the exact coarse/fine subtraction carries an absolute error of
-// ~2^-43 whatever the operands' size, ~20 times the TwoSum form's on typical
-// terms, and the terms with a small Re(wdiff) -- the largest ones -- would
-// carry it into the sum (tests/test_error_budget.py: 2e-11 against 8e-13 on
-// a sum of production-like terms, the same 8e-13 with this radius).
-constexpr float kNearRadius = 0.5f;
-// Mask bits of every bucket a wtilde within kNearRadius plus the FP64 pole
-// distance of x (|wdiff|^2 < 1e-6 x^2, so |x - Re(wtilde)| < 1e-3 |x|) can
-// fall into, with a margin far above the float rounding of both sides; all
-// bits for NaN.
-__host__ __device__ __forceinline__ unsigned long long near_buckets(float x) {
-    const float rad = kNearRadius + 1.01e-3f * fabsf(x) + 1e-30f;
+// Mask bits of every bucket a wtilde within the FP64 pole distance of x
+// (|wdiff|^2 < 1e-6 x^2, so |x - Re(wtilde)| < 1e-3 |x|) can fall into, with
+// a margin far above the float rounding of both sides; all bits for NaN.
+__host__ __device__ __forceinline__ unsigned long long pole_buckets(float x) {
+    const float rad = 1.01e-3f * fabsf(x) + 1e-30f;
     const float lo = x - rad, hi = x + rad;
     if (!(lo <= hi)) return ~0ull;
     const unsigned c0 = bucket_code(lo), c1 = bucket_code(hi);
@@ -169,37 +152,27 @@ static __device__ __noinline__ TermPair pole_pair(const Problem &p, df2 d, float
     return t;
 }
 
-// How a column routine forms Re(wdiff), and whether it tests for the pole.
-enum : int {
-    kColExact = 0,    // coarse/fine operands at least kNearRadius apart: exact subtraction
-    kColGeneral = 1,  // TwoSum of any df operands, with the per-term pole test
-};
-
 // The df arithmetic of one ig column for one warp: RNW bands x the tile's
 // two rows x NWC frequencies of aqsn * Q * conj(wdiff) / |wdiff|^2 added into
 // acc.  Every value is a df2 whose lanes are rows row0 and row0 + 1, so one
 // packed f32x2 instruction advances both rows' terms; the row-pair planes
 // load straight into lane pairs and band values broadcast to both lanes.
-// Re(wdiff) = wx - Re(wtilde): with both in coarse/fine form and at least
-// kNearRadius apart (MODE kColExact) the main parts subtract exactly and
-// the fine parts round once (2 packed instructions); otherwise (kColGeneral)
-// a TwoSum of the df values (8).  Either way it is renormalised after its
-// cancelling subtraction, and the reciprocal carries a second-order
-// correction, folded into the two products by 1/|wdiff|^2: both keep the
-// per-term error near 2^-44 relative and free of a sign preference (an
-// unnormalised wdiff or a first-order reciprocal biases every term the same
-// way, and sums of 1e10 terms turn a 1e-15 bias into 1e-10).  kColGeneral
-// tests every term for the pole and recomputes those within 1e-3 |wx| of it
-// in FP64 from the inputs; kColExact needs no test, its terms being at least
-// kNearRadius from the pole.
-template <int RNW, int NWC, int KC, int MODE>
+// Re(wdiff) is renormalised after its cancelling subtraction and the
+// reciprocal carries a second-order correction, folded into the two
+// products by 1/|wdiff|^2 (df2_mul_rcp): both keep the per-term error near
+// 2^-44 relative and free of a sign preference (an unnormalised wdiff or a
+// first-order reciprocal biases every term the same way, and sums of 1e10
+// terms turn a 1e-15 bias into 1e-10; tests/test_error_budget.py measures
+// each step).  With CHECK, terms within 1e-3 |wx| of the pole are
+// recomputed in FP64 from the inputs; tiles call the CHECK = false form only
+// when no wtilde can come that near any of the warp's wx values.
+template <int RNW, int NWC, int KC, bool CHECK>
 __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
                                              const float4 *sb, int il, int ig, int row0,
                                              int bandw, int band_end, int iw0,
                                              const df (&wx)[RNW][NWC],
                                              const float (&pole_thr)[RNW][NWC],
                                              df2 (&acc)[RNW][NWC][2]) {
-    constexpr bool CHECK = MODE == kColGeneral;
     const float4 vr = st[il], vi = st[KC + il], vqr = st[2 * KC + il], vqi = st[3 * KC + il];
     const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)};
     const df2 wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
@@ -217,14 +190,8 @@ __device__ __forceinline__ void mixed_column(const Problem &p, const float4 *st,
         const df2 Ar_wti = df2_mul(Ar, wti);
 #pragma unroll
         for (int w = 0; w < NWC; ++w) {
-            df2 wr;  // Re(wdiff)
-            if (MODE == kColGeneral) {
-                wr = df2_norm(df2_sub(df2_bcast(wx[n][w]), wtr));
-            } else {
-                const df2 x = df2_bcast(wx[n][w]);
-                wr = df2_norm({f2sub(x.h, wtr.h), f2sub(x.l, wtr.l)});
-            }
-            const df2 d = df2_add(df2_sqr(wr), wti2);  // |wdiff|^2
+            const df2 wr = df2_norm(df2_sub(df2_bcast(wx[n][w]), wtr));  // Re(wdiff)
+            const df2 d = df2_add(df2_sqr(wr), wti2);                     // |wdiff|^2
             float2 r0, rc;                              // 1/d = r0 (1 + rc)
             df2_rcp_parts(d, r0, rc);
             // A conj(wdiff) / |wdiff|^2, conj(wdiff) = (wr, wti)
@@ -337,8 +304,7 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
 
     df wx[RNW][NWC];
     float pole_thr[RNW][NWC];
-    unsigned long long near_mask = 0;  // value buckets of a wtilde near a wx of this warp
-    bool general = false;              // a wx of this warp is not in coarse/fine form
+    unsigned long long pole_mask = 0;  // value buckets of a possible pole term
     const unsigned long long *mask_row =
         s.masks + (size_t)row_tile * ((nc + kMaskCols - 1) / kMaskCols);
 #pragma unroll
@@ -348,10 +314,8 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
         for (int w = 0; w < NWC; ++w) {
             const float2 x = s.wx[(size_t)b * p.nw + min(iw0 + w, p.nw - 1)];
             wx[n][w] = {x.x, x.y};
-            const float xn = fadd(x.x, x.y);  // nearest float to wx
-            pole_thr[n][w] = 1e-6f * xn * xn;  // |wdiff|^2 < (1e-3 |wx|)^2
-            near_mask |= near_buckets(xn);
-            general |= !(fabsf(x.x) <= kCoarseBound);
+            pole_thr[n][w] = 1e-6f * x.x * x.x;  // |wdiff|^2 < (1e-3 |wx|)^2
+            pole_mask |= pole_buckets(x.x);
         }
     }
     df2 acc[RNW][NWC][2];  // lanes: the two rows
@@ -391,16 +355,16 @@ __device__ __forceinline__ bool mixed_tile(const Problem &p, const Partials &par
             const float4 *sb = st + (2 * RG + warp * RNW) * KC;  // this warp's bands
             const int k0 = c * KC;
             const int cnt = min(KC, nc - k0);
-            if (general || (chunk_mask & (near_mask | kWideBit))) {
+            if (chunk_mask & pole_mask) {
 #pragma unroll kColUnroll
                 for (int il = lane; il < cnt; il += 32)
-                    mixed_column<RNW, NWC, KC, kColGeneral>(p, st, sb, il, k0 + il, row0, bandw,
-                                                            band_end, iw0, wx, pole_thr, acc);
+                    mixed_column<RNW, NWC, KC, true>(p, st, sb, il, k0 + il, row0, bandw,
+                                                     band_end, iw0, wx, pole_thr, acc);
             } else {
 #pragma unroll kColUnroll
                 for (int il = lane; il < cnt; il += 32)
-                    mixed_column<RNW, NWC, KC, kColExact>(p, st, sb, il, k0 + il, row0, bandw,
-                                                          band_end, iw0, wx, pole_thr, acc);
+                    mixed_column<RNW, NWC, KC, false>(p, st, sb, il, k0 + il, row0, bandw,
+                                                      band_end, iw0, wx, pole_thr, acc);
             }
         }
         if (SYNC == kSyncBlock) {
@@ -563,8 +527,7 @@ __device__ __forceinline__ void flag_mixed_tile(const Problem &p, const Partials
         const float4 pqr = __ldg(rp + 2 * nc + ig), pqi = __ldg(rp + 3 * nc + ig);
 #pragma unroll
         for (int g = 0; g < RG; ++g) {
-            // Re(wtilde) may be in coarse/fine form: renormalised to (hi, lo).
-            const df wtr = df_norm(pair_lane(pwr, g)), wti = pair_lane(pwi, g);
+            const df wtr = pair_lane(pwr, g), wti = pair_lane(pwi, g);
             const df qr = pair_lane(pqr, g), qi = pair_lane(pqi, g);
             const df wti2 = df_sqr(wti);
             const df awt2 = df_add(df_sqr(wtr), wti2);                         // |wtilde|^2

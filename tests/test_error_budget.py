@@ -11,18 +11,24 @@ relative error of the sum of all terms (accumulated in long double, so only
 the per-term error shows), the RMS per-term relative error and the mean
 signed per-term error (a sign preference, which long sums amplify).
 
-Variants: the shipped form (Re(wdiff) by the exact coarse/fine subtraction
-where |Re(wdiff)| >= 0.5, by TwoSum elsewhere; the reciprocal folded into
-the products); the earlier TwoSum-everywhere form; the exact subtraction
-everywhere and at other radii; and the shipped form with one step at a time
-done in plain FP32 (its low part dropped).  The benchmark's bound is 1e-8
-per component and the kernels deliver ~1e-12; a step may leave float-float
-only if doing so keeps the sum within 1e-10.  None does: every FP32 step
-puts ~1e-8 to 1e-7 into the sum, because with random-sign terms the
-relative error of the sum is the per-term relative error itself.  The exact
-subtraction everywhere costs a factor ~25 on the sum (its ~2^-43 absolute
-error weighs on the large small-Re(wdiff) terms); from radius 0.25 on it
-costs nothing measurable.
+Variants: the shipped form (Re(wdiff) by TwoSum, the reciprocal's
+second-order correction folded into the two products); the earlier form
+with a separate df reciprocal; an exact coarse/fine subtraction for
+Re(wdiff) (main parts on a 2^-18 grid, two packed instructions instead of
+eight), everywhere and only where |Re(wdiff)| >= 0.25, 0.5, 1; and the
+shipped form with one step at a time done in plain FP32 (its low part
+dropped).  The benchmark's bound is 1e-8 per component and the kernels
+deliver ~1e-12; a step may leave float-float only if doing so keeps the sum
+within 1e-10.  None does: every FP32 step puts ~1e-8 to 1e-7 into the sum,
+because with random-sign terms the relative error of the sum is the
+per-term relative error itself.  The exact subtraction everywhere costs a
+factor ~25 on the sum (its ~2^-43 absolute error weighs on the large terms
+of small Re(wdiff)); confined to |Re(wdiff)| >= 0.5 it costs nothing here,
+but only if the other terms keep the full (hi, lo) Re(wtilde) -- in the
+kernel they read the same planes, and a trial that stored the coarse/fine
+form alone lost precision on every near-pole term (6e-10 on the 32-frequency
+long sums, against 5e-11) while gaining 2% of kernel time, so it was not
+kept.
 
     python tests/test_error_budget.py [terms]   # prints the table
 """
@@ -66,11 +72,11 @@ static double uni(void) {  /* SplitMix64 */
     z ^= z >> 31; return (z >> 11) * (1.0 / 9007199254740992.0);
 }
 
-enum { V_SHIPPED, V_TWOSUM, V_EXACT, V_H025, V_H1, V_A, V_AWTI, V_WTI2, V_WDIFF, V_D, V_RCP1, V_RCP, V_NUM, V_PROD, NV };
+enum { V_SHIPPED, V_TWOSUM, V_EXACT, V_H025, V_H05, V_H1, V_A, V_AWTI, V_WTI2, V_WDIFF, V_D, V_RCP1, V_RCP, V_NUM, V_PROD, NV };
 static const char *names[NV] = {
-    "shipped: exact where |Re(wdiff)| >= 0.5", "TwoSum Re(wdiff), separate reciprocal",
+    "shipped: TwoSum Re(wdiff), fused reciprocal", "separate df reciprocal",
     "exact Re(wdiff) everywhere", "exact where |Re(wdiff)| >= 0.25",
-    "exact where |Re(wdiff)| >= 1",
+    "exact where |Re(wdiff)| >= 0.5", "exact where |Re(wdiff)| >= 1",
     "FP32: A = aqsn Q", "FP32: A Im(wtilde)", "FP32: Im(wtilde)^2", "FP32: Re(wdiff)",
     "FP32: |wdiff|^2", "first-order reciprocal", "FP32: reciprocal", "FP32: numerator sums",
     "FP32: products by 1/|wdiff|^2"};
@@ -85,10 +91,11 @@ static void term(int v, df ar, df ai, df wtr, df wti, df qr, df qi, df wx, long 
     df Ai_wti = df_mul(Ai, wti), Ar_wti = df_mul(Ar, wti);
     if (v == V_AWTI) { Ai_wti = f32(Ai_wti); Ar_wti = f32(Ar_wti); }
     df wr;
-    /* The kernel's chunk test (value buckets) is coarser than this per-term
-       one: it only ever sends more terms to the general form. */
-    const float far = v == V_H025 ? 0.25f : v == V_H1 ? 1.0f : v == V_EXACT ? 0.f : 0.5f;
-    if (v == V_TWOSUM || (far > 0.f && !(fabsf(wx.h - wtr.h) >= far))) {
+    /* The exact subtraction (rejected): everywhere, or only at least `far`
+       from the pole with TwoSum on the full (hi, lo) values elsewhere. */
+    const int exact = v == V_EXACT || v == V_H025 || v == V_H05 || v == V_H1;
+    const float far = v == V_H025 ? 0.25f : v == V_H05 ? 0.5f : v == V_H1 ? 1.0f : 0.f;
+    if (!exact || (far > 0.f && !(fabsf(wx.h - wtr.h) >= far))) {
         wr = df_norm(df_sub(wx, wtr));
     } else {
         df x = wx, t = wtr;
@@ -104,7 +111,7 @@ static void term(int v, df ar, df ai, df wtr, df wti, df qr, df qi, df wx, long 
     df nre = df_sub(df_mul(Ar, wr), Ai_wti), nim = df_add(df_mul(Ai, wr), Ar_wti);
     if (v == V_NUM) { nre = (df){Ar.h * wr.h - Ai_wti.h, 0.f}; nim = (df){Ai.h * wr.h + Ar_wti.h, 0.f}; }
     df tre, tim;
-    if (v == V_TWOSUM) {  /* df_mul by the df reciprocal (r0, r0 c) */
+    if (v == V_TWOSUM) {  /* the earlier form: df_mul by the df reciprocal (r0, r0 c) */
         df r = {r0, r0 * c}; tre = df_mul(nre, r); tim = df_mul(nim, r);
     } else {
         float p = nre.h * r0, q = fmaf(nre.h, r0, -p); q = fmaf(p, c, q); q = fmaf(nre.l, r0, q); tre = (df){p, q};
@@ -186,15 +193,15 @@ def run_table(tmp_path, terms: int) -> dict:
 
 def test_no_step_of_the_term_can_leave_float_float(tmp_path):
     rows, text = run_table(tmp_path, 1_000_000)
-    shipped = rows["shipped: exact where |Re(wdiff)| >= 0.5"]
-    twosum = rows["TwoSum Re(wdiff), separate reciprocal"]
+    shipped = rows["shipped: TwoSum Re(wdiff), fused reciprocal"]
+    separate = rows["separate df reciprocal"]
     everywhere = rows["exact Re(wdiff) everywhere"]
-    # The shipped form and the earlier one: per-term error ~2^-44, no bias,
+    # The shipped form and the earlier one: per-term error ~2^-47, no bias,
     # the same error on the sum.
-    for r in (shipped, twosum):
+    for r in (shipped, separate):
         assert r[0] <= 1e-11 and r[1] <= 1e-13 and abs(r[2]) <= 1e-15, text
-    assert shipped[0] <= 2 * twosum[0], text
-    # Why the exact subtraction is confined to |Re(wdiff)| >= 0.5.
+    assert shipped[0] <= 2 * separate[0], text
+    # Why the exact subtraction is not used everywhere.
     assert everywhere[0] > 5 * shipped[0], text
     for name, r in rows.items():
         if name.startswith("FP32:"):

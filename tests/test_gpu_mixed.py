@@ -81,26 +81,45 @@ def test_production_near_pole_mixed_within_1e8_of_fp64():
     assert ea <= MIXED_TOL and ex <= MIXED_TOL
 
 
-def test_every_pipeline_variant_gives_the_same_bits_and_autotune_picks_one():
+@pytest.mark.parametrize("nw", [3, 8])
+def test_every_variant_matches_the_oracle_and_autotune_picks_one(nw):
+    """Every compiled variant -- tile shape (bands x rows per block) and
+    shared-memory pipeline -- against the oracle within the mixed bound,
+    bit-identical to the other variants of its shape (the pipeline does not
+    change the order of the sums; the shape does) and to its own rerun."""
+    import oracle_py
     o = ops()
-    shape = W.Shape(20, 2, 3000, 40, 3, near_pole=0.01)
-    d = o.DeviceInputs.from_host(W.make_inputs(shape, 9))
-    ref = None
+    lib = capi.load()
+    shape = W.Shape(20, 2, 3000, 40, nw, near_pole=0.01)
+    inp = W.make_inputs(shape, 9)
+    want = oracle_py.run(inp, "complex_seq", nthreads=4)
+    d = o.DeviceInputs.from_host(inp)
     names = o.variant_names()
-    assert len(names) >= 2
+    assert len(names) >= 8
+    by_shape = {}
+    tried = 0
     try:
         for v in range(len(names)):
-            o.set_variant(3, v)
+            if lib.gpp_set_variant(nw, v) != capi.GPP_OK:
+                continue  # not compiled for this frequency chunk
+            tried += 1
             r = o.sigma(d, "mixed")
+            r2 = o.sigma(d, "mixed")
             o.wait()
             got = torch.view_as_real(r.achtemp).cpu()
-            if ref is None:
-                ref = got
-            assert torch.equal(got, ref), names[v]
+            assert torch.equal(got, torch.view_as_real(r2.achtemp).cpu()), names[v]
+            assert rel_err(r.achtemp.cpu().numpy(), want["achtemp"]) <= MIXED_TOL, names[v]
+            assert rel_err(r.asxtemp.cpu().numpy(), want["asxtemp"]) <= MIXED_TOL, names[v]
+            key = names[v].split(",")[0]
+            if key in by_shape:
+                assert torch.equal(got, by_shape[key]), names[v]
+            else:
+                by_shape[key] = got
+        assert tried >= 2 and len(by_shape) >= 2
         best = o.autotune(d, max_bands=8)
-        assert 0 <= best < len(names)
+        assert lib.gpp_set_variant(nw, best) == capi.GPP_OK
     finally:
-        o.set_variant(3, -1)
+        o.set_variant(nw, -1)
 
 
 @pytest.mark.parametrize("semantics", ["complex_seq", "kerseq"])
