@@ -742,12 +742,19 @@ struct gpp_context {
 // the unoccupied-band kernel.
 constexpr int kHostPieceCuts[] = {1, 5, 16};
 
-// How gpp_sigma_host moves its inputs: 0 = copy engine (default), 1 = SM
-// pull kernel (GPP_HOST_PULL=sm).
+// How gpp_sigma_host moves inputs the device can address (pinned host
+// memory): 1 = an SM pull kernel (default), 0 = the copy engine
+// (GPP_HOST_PULL=ce).  Measured on GB300 at the production shape from
+// pinned memory, copy-engine copies ran either at ~210 GB/s or at 10-40 GB/s,
+// alternating between back-to-back calls and always slow after the GPU had
+// been idle for a fraction of a second (calls of 218 or 263-287 ms); the
+// pull kernel moved the same 2.25 GB in 10.7-11 ms on every call, and the
+// call took 224 ms back to back and after idle pauses alike.  Pageable
+// memory always goes through the copy engine.
 int host_pull_mode() {
     static const int mode = [] {
         const char *v = getenv("GPP_HOST_PULL");
-        return (v && strcmp(v, "sm") == 0) ? 1 : 0;
+        return (v && strcmp(v, "ce") == 0) ? 0 : 1;
     }();
     return mode;
 }
@@ -799,7 +806,12 @@ gpp_status gpp_context_create(gpp_context **ctx) {
     gpp_context *c = new gpp_context();
     cudaError_t e = cudaGetDevice(&c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
+    // The copy stream at the highest priority: a pull kernel (GPP_HOST_PULL=sm)
+    // on it is scheduled ahead of the computation's blocks.
+    int prio_lo = 0, prio_hi = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithPriority(&c->copy, cudaStreamNonBlocking, prio_hi);
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
     for (int i = 0; i < kMaxRowPieces && e == cudaSuccess; ++i)
         e = cudaEventCreateWithFlags(&c->ready[i], cudaEventDisableTiming);
@@ -859,10 +871,11 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     }
     char *d = static_cast<char *>(ctx->dev);
     ctx->timed = false;
-    // Transfers: copy engine by default; with GPP_HOST_PULL=sm the SMs pull
-    // every input the device can address (pinned host memory, 16-byte
-    // aligned) with a kernel on the copy stream, before the computation (the
-    // computation's blocks fill the SMs, so the pull gets no room beside it).
+    // Transfers: the SMs pull every input the device can address (pinned
+    // host memory, 16-byte aligned) with a kernel on the copy stream (highest
+    // priority, so its blocks take SM slots as the computation's blocks
+    // retire); anything else, or everything with GPP_HOST_PULL=ce, goes
+    // through the copy engine.
     const bool sm_pull = host_pull_mode() == 1;
     std::vector<const char *> src_dev(in.size(), nullptr);
     if (sm_pull)
@@ -891,7 +904,7 @@ gpp_status gpp_sigma_host(gpp_context *ctx, const gpp_problem *problem, const gp
     const int pairs = (int)((ng + 1) / 2);
     pieces.n = 0;
     pieces.pair[0] = 0;
-    for (int cut : (sm_pull ? std::vector<int>{16} : host_piece_cuts())) {
+    for (int cut : host_piece_cuts()) {
         const int b = (int)((long long)pairs * cut / 16);
         if (b > pieces.pair[pieces.n]) pieces.pair[++pieces.n] = b;
     }

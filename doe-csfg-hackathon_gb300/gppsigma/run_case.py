@@ -21,6 +21,9 @@ from gppsigma import workload as W  # noqa: E402
 # Extra shapes for profiling: larger than L2 (129 MB), a few hundred MB total.
 SHAPES = dict(W.CONFIGS)
 SHAPES["profile"] = W.Shape(512, 2, 8192, 512, 3, near_pole=0.01)
+# The 32-frequency sweep's distributions and ncouls at a fraction of its bands
+# and rows (~2 GB on the device with the split planes): the 8-frequency tile.
+SHAPES["sweep32_small"] = W.Shape(64, 8, 65536, 400, 32, dw=0.25)
 
 
 def main() -> int:

@@ -146,10 +146,10 @@ int gpp_get_dropin_precision(void);
  * the band-sum GEMM when there are at least 32 unoccupied bands, 0 always
  * with the per-term kernel, 1 always through the GEMM.  With wx the same
  * for every band the band sum factors out of the division:
- * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM:
- * cuBLAS in FP64, a float-float GEMM on the FP32 pipes in mixed precision),
- * several times faster; the results agree with the per-term kernels to
- * their rounding. */
+ * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM,
+ * written in this library: 3M-form FP64 on the FP64 pipe, float-float on the
+ * FP32 pipes in mixed precision), several times faster; the results agree
+ * with the per-term kernels to their rounding. */
 gpp_status gpp_set_gemm_path(int mode);
 
 /* ------------------------------------------------------------------------
@@ -193,10 +193,14 @@ gpp_status gpp_sigma(const gpp_problem *problem, const gpp_outputs *out, gpp_str
 gpp_status gpp_wait(gpp_stream_t stream, int timeout_ms);
 
 /* Host-memory convenience path (end-to-end): every array pointer in
- * `problem` is a HOST pointer (pinned memory gives full copy speed), as are
- * the outputs.  The call copies inputs to device buffers owned by `ctx`, runs
- * gpp_sigma on the context's stream, copies results back and returns when
- * they are on the host. */
+ * `problem` is a HOST pointer, as are the outputs.  The call moves the inputs
+ * to device buffers owned by `ctx` -- pinned (device-mapped) arrays by a
+ * pull kernel on the SMs, overlapped with the computation in row pieces;
+ * pageable ones, or all of them with GPP_HOST_PULL=ce in the environment, by
+ * the copy engine -- runs gpp_sigma on the context's stream, copies results
+ * back and returns when they are on the host.  Pinned memory is the fast
+ * input: on GB300 the pull moves it at ~210 GB/s on every call, while
+ * copy-engine copies were seen alternating with 10-40 GB/s calls. */
 typedef struct gpp_context gpp_context;
 gpp_status gpp_context_create(gpp_context **ctx);
 gpp_status gpp_context_destroy(gpp_context *ctx);
