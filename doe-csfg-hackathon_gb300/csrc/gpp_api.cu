@@ -456,13 +456,18 @@ Problem to_problem(const gpp_problem &q) {
     return p;
 }
 
-// Grid limits of one call's launches: grid.y of the unoccupied-band kernels
-// counts band tiles, grid.y of the occupied-band kernels counts occupied
-// bands, grid.z counts frequency chunks; each must stay <= 65535.
+// Grid limits of one call's launches: the unoccupied-band kernels' grid.x
+// counts (row tile, band tile) pairs (<= 2^31 - 1) and their band tiles are
+// kept <= 65535; grid.y of the occupied-band kernels counts occupied bands,
+// and frequency chunks stay <= 65535.
 gpp_status check_grid_limits(const Problem &p, int occupied_bands, int unoccupied_bands,
                              const TileShape &ns, bool gemm) {
     if (unoccupied_bands > 0 && !gemm && ceil_div(unoccupied_bands, ns.rn) > 65535)
         return fail(GPP_ERR_UNSUPPORTED, "too many bands for one launch (%d)", unoccupied_bands);
+    // The per-term kernels walk (row tile, band tile) pairs along grid.x.
+    if (unoccupied_bands > 0 && !gemm &&
+        (long long)ceil_div(p.ng, ns.rg) * ceil_div(unoccupied_bands, ns.rn) > 2147483647LL)
+        return fail(GPP_ERR_UNSUPPORTED, "too many tiles for one launch");
     if (ceil_div(p.nw, ns.nwc) > 65535 || occupied_bands > 65535)
         return fail(GPP_ERR_UNSUPPORTED, "too many frequencies or occupied bands");
     return GPP_OK;

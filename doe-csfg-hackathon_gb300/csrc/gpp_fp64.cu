@@ -9,6 +9,7 @@
 #include <cstdio>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "gpp_kernels.h"
 #include "gpp_tiles_fp64.cuh"
@@ -17,16 +18,28 @@ namespace gpp {
 
 namespace {
 
+// Row tiles per group of the tile order: a group's G' rows (16 row pairs,
+// 32 MB at ncouls 32768) stay in L2 while every band tile streams past
+// them, so each row is read from HBM about once per launch and each band
+// once per group, instead of every row once per band tile.
+constexpr int kFp64Group = 16;
+
 template <int RN, int RG, int NWC, int THREADS>
 __global__ void __launch_bounds__(THREADS)
 noflag_fp64_kernel(Problem p, Partials part, int band_begin, int band_end, int row_tile0,
-                   int row_tiles) {
+                   int rows_here, int row_tiles, int band_tiles) {
     constexpr int K = RN * RG * NWC * 2;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    const int row_tile = row_tile0 + blockIdx.x;
-    noflag_fp64_tile<RN, RG, NWC, THREADS>(p, part, band_begin, band_end, row_tile, blockIdx.y,
-                                           blockIdx.z, (long long)blockIdx.y * row_tiles + row_tile,
+    // Grouped order over this launch's row tiles [row_tile0, +rows_here).
+    const int tiles_per_group = kFp64Group * band_tiles;
+    const int grp = blockIdx.x / tiles_per_group;
+    const int in_grp = blockIdx.x - grp * tiles_per_group;
+    const int rows_in_grp = min(kFp64Group, rows_here - grp * kFp64Group);
+    const int row_tile = row_tile0 + grp * kFp64Group + in_grp % rows_in_grp;
+    const int band_tile = in_grp / rows_in_grp;
+    noflag_fp64_tile<RN, RG, NWC, THREADS>(p, part, band_begin, band_end, row_tile, band_tile,
+                                           blockIdx.y, (long long)band_tile * row_tiles + row_tile,
                                            red, S);
 }
 
@@ -100,9 +113,10 @@ cudaError_t launch_noflag_t(const Problem &p, const Partials &part, int b0, int 
     const int row_tiles = ceil_div(p.ng, RG);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
-    dim3 grid(r.end - r.begin, ceil_div(b1 - b0, RN), ceil_div(p.nw, NWC));
-    noflag_fp64_kernel<RN, RG, NWC, THREADS><<<grid, THREADS, 0, s>>>(p, part, b0, b1, r.begin,
-                                                                       row_tiles);
+    const int band_tiles = ceil_div(b1 - b0, RN);
+    dim3 grid((unsigned)((long long)(r.end - r.begin) * band_tiles), ceil_div(p.nw, NWC));
+    noflag_fp64_kernel<RN, RG, NWC, THREADS><<<grid, THREADS, 0, s>>>(
+        p, part, b0, b1, r.begin, r.end - r.begin, row_tiles, band_tiles);
     count_launch();
     return cudaGetLastError();
 }
@@ -272,9 +286,17 @@ cudaError_t launch_host_pull(void *dst, const void *src_dev, size_t bytes, cudaS
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // Blocks per SM: GPP_HOST_PULL_BLOCKS (1..16), default 4 -- enough loads
+    // in flight for the link; fewer leave more room to a computation that
+    // runs beside the pull.
+    static const int per_sm = [] {
+        const char *v = getenv("GPP_HOST_PULL_BLOCKS");
+        const int k = v ? atoi(v) : 4;
+        return (k >= 1 && k <= 16) ? k : 4;
+    }();
     const size_t words = bytes / 16;
     const size_t want = (words + 255) / 256;
-    const int grid = (int)std::min<size_t>(want, (size_t)std::max(1, sms) * 4);
+    const int grid = (int)std::min<size_t>(want, (size_t)std::max(1, sms) * per_sm);
     host_pull_kernel<<<grid, 256, 0, s>>>(static_cast<uint4 *>(dst),
                                            static_cast<const uint4 *>(src_dev), words);
     count_launch();
