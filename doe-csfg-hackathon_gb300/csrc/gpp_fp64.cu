@@ -196,7 +196,7 @@ cudaError_t launch_reduce(const double2 *src, long long stride, int len, int nse
 namespace {
 // Host-to-device transfer by the SMs: each thread streams 16-byte words
 // from host memory the device can address (pinned, mapped into the device's
-// address space) into device memory.  The alternative to a copy-engine
+// address space) into device memory, over NVLink-C2C on GB300.  The alternative to a copy-engine
 // cudaMemcpyAsync for the host path (gpp_sigma_host); `bytes` is a multiple
 // of 16 and both pointers are 16-byte aligned (the caller checks).
 __global__ void __launch_bounds__(256) host_pull_kernel(uint4 *__restrict__ dst,
@@ -286,13 +286,15 @@ cudaError_t launch_host_pull(void *dst, const void *src_dev, size_t bytes, cudaS
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // Blocks per SM: GPP_HOST_PULL_BLOCKS (1..16), default 4 -- enough loads
-    // in flight for the link; fewer leave more room to a computation that
-    // runs beside the pull.
+    // Blocks per SM: GPP_HOST_PULL_BLOCKS (1..16), default 1.  One block of
+    // 256 threads per SM, four 16-byte loads in flight per thread, keeps
+    // ~2.5 MB in flight -- enough for the link -- and leaves the most room to
+    // the computation running beside the pull (GB300, production shape:
+    // 221.3 ms per host-path call with 1 block per SM, 224.4 ms with 4).
     static const int per_sm = [] {
         const char *v = getenv("GPP_HOST_PULL_BLOCKS");
-        const int k = v ? atoi(v) : 4;
-        return (k >= 1 && k <= 16) ? k : 4;
+        const int k = v ? atoi(v) : 1;
+        return (k >= 1 && k <= 16) ? k : 1;
     }();
     const size_t words = bytes / 16;
     const size_t want = (words + 255) / 256;
