@@ -151,18 +151,29 @@ def test_device_side_index_fault_is_reported_then_cleared():
         o.wait()
 
 
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("ngpown", [20, 3, 33])
-def test_host_path_equals_device_path(precision, ngpown):
-    """The host path copies the G' rows in pieces and starts each piece's
-    kernels when its rows land; the bits must equal one device-path call."""
+def test_host_path_equals_device_path(precision, ngpown, memory):
+    """The host path moves the G' rows in pieces and starts each piece's
+    kernels when its rows land; the bits must equal one device-path call.
+    Pinned arrays are pulled by the SMs (those whose size is not a multiple
+    of 16 bytes -- inv_igp_index at 3 and 33 rows -- go through the copy
+    engine beside them); pageable ones through the copy engine."""
     o = ops()
     inp = W.make_inputs(W.Shape(12, 3, 1000, ngpown, 3, near_pole=0.05), 51)
     d = o.DeviceInputs.from_host(inp)
     dev = o.sigma(d, precision, acht_n1=True, achstemp=True)
     o.wait()
-    arrays = {k: getattr(inp, k) for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array",
-                                           "vcoul", "inv_igp_index", "indinv", "wx_array")}
+    keep = {}
+    arrays = {}
+    for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul", "inv_igp_index",
+              "indinv", "wx_array"):
+        a = np.ascontiguousarray(getattr(inp, k))
+        if memory == "pinned":
+            keep[k] = torch.from_numpy(a).pin_memory()
+            a = keep[k].numpy()
+        arrays[k] = a
     with o.HostContext() as ctx:
         with pytest.raises(capi.GppError):
             ctx.last_timing()  # nothing timed yet
