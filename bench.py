@@ -434,6 +434,9 @@ def main() -> int:
         d = ops.device_inputs(shape, gdist.state_seed(SEED, rank))
         job_terms = ws * shape.terms
     stream = torch.cuda.current_stream()
+    input_gb = sum(getattr(d, k).numel() * getattr(d, k).element_size()
+                   for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul",
+                             "inv_igp_index", "wx_array")) / 1e9
     nterms = shape.terms
     unocc_terms = (shape.number_bands - shape.nvband) * shape.ngpown * shape.ncouls * shape.nw
 
@@ -603,7 +606,7 @@ def main() -> int:
             "data": "synthetic (seeded SplitMix64, reference distributions)",
             "config": {"workload": args.workload, **shape_dict(full_shape), "precision": precision,
                        "mixed_variant": variant,
-                       "l2": "inputs (2.25 GB) larger than L2 (129 MB)",
+                       "l2": f"inputs ({input_gb:.2f} GB) larger than L2 (129 MB)",
                        "parallelism": (f"one state, G' rows split over {ws} GPU(s), partial "
                                        "sums added on rank 0 in rank order"
                                        if args.shard == "rows" else
