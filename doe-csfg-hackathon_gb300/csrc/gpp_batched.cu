@@ -145,8 +145,11 @@ __host__ __device__ constexpr int batch_kc() { return NWC <= 4 ? 192 : 256; }
 // frequencies, 3 (168 registers) for the 8-frequency tile.  Left to the
 // compiler's heuristic, the persistent loop takes 158 and 254 registers and
 // a quarter to a third of the warps.
-template <int RG, int NWC>
-__global__ void __launch_bounds__(kThreads, NWC <= 4 ? 4 : 3)
+// NWARP warps per block, one band each: 4 (the default tile, 4 bands x 2
+// rows) or 8 (8 bands x 2 rows), following the tile shape the autotuner
+// chose for single states; the same register budget per thread either way.
+template <int RG, int NWC, int NWARP = 4>
+__global__ void __launch_bounds__(NWARP * 32, (NWC <= 4 ? 4 : 3) * 4 / NWARP)
 batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const SplitPlanes *splits,
                             const BatchItem *items, int n_items, int *head) {
     __shared__ int s_item;
@@ -161,7 +164,7 @@ batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const S
         const Problem p = probs[bi.state];
         const Partials part = parts[bi.state];
         const SplitPlanes sp = splits[bi.state];
-        if (!mixed_tile<1, RG, NWC, 4, batch_kc<NWC>(), 2, kSyncBlock>(
+        if (!mixed_tile<1, RG, NWC, NWARP, batch_kc<NWC>(), 2, kSyncBlock>(
                 p, part, sp, p.nv, p.nb, bi.row_tile, bi.band_tile, bi.iw_chunk, bi.tile, reinit))
             return;  // abandoned after a bounded wait; the fault bit is set
         reinit = true;
@@ -170,11 +173,11 @@ batched_noflag_mixed_kernel(const Problem *probs, const Partials *parts, const S
 }
 
 template <typename K>
-int resident_blocks(K kern, size_t smem) {
+int resident_blocks(K kern, size_t smem, int threads = kThreads) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kThreads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem);
     return std::max(1, sms) * std::max(1, per);
 }
 
@@ -217,6 +220,7 @@ struct gpp_batch {
     std::vector<int> achs_blocks;
     std::vector<std::pair<double2 *, size_t>> n1_zero;
     int launches_per_run = 0;
+    int warps = 4;    // warps (bands) per unoccupied-band block of the mixed path
     size_t smem = 0;  // persistent kernel: dynamic shared memory per block
     int grid = 1;       // persistent kernels: resident blocks on the device
     int grid_flag = 1;
@@ -258,10 +262,19 @@ gpp_status plan_batch(gpp_batch *b, const gpp_problem *problems, const gpp_outpu
     Problem p0{};
     p0.nw = nw;
     const TileShape fs = flag_shape(p0);
-    // The persistent unoccupied-band kernel is compiled in the default
-    // variant's shape (4 bands x 2 rows).
-    const TileShape ns =
-        mixed ? mixed_noflag_shape(p0, mixed_default_variant()) : fp64_noflag_shape(p0);
+    // The unoccupied-band tile shape of the mixed path follows the tuned
+    // variant where the persistent kernel is compiled in that shape (4 or 8
+    // warps of one band; 8 for 3- and 8-frequency chunks); otherwise, and for
+    // a two-bands-per-warp choice, 4 bands x 2 rows.
+    TileShape ns = fp64_noflag_shape(p0);
+    if (mixed) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+        ns = mixed_noflag_shape(p0, tuned_mixed_variant(dev, nw));
+        const bool eight = ns.threads == 256 && ns.rn == 8 && (nwc == 3 || nwc == 8);
+        if (!eight) ns = mixed_noflag_shape(p0, mixed_default_variant());
+        b->warps = eight ? 8 : 4;
+    }
 
     struct StateGeom {
         long long rows_f, rows_n, tiles_f, tiles_n, ach_seg, n1_seg;
@@ -474,12 +487,24 @@ template <int NWC>
 cudaError_t prepare_persistent(gpp_batch *b) {
     if (b->precision == GPP_PRECISION_MIXED) {
         constexpr int RG = 2;  // one row pair of the split planes
-        auto kern = batched_noflag_mixed_kernel<RG, NWC>;
-        b->smem = sizeof(float4) * 2 * (2 * RG + 4) * batch_kc<NWC>();
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)b->smem);
-        if (e != cudaSuccess) return e;
-        b->grid = resident_blocks(kern, b->smem);
+        b->smem = sizeof(float4) * 2 * (2 * RG + b->warps) * batch_kc<NWC>();
+        cudaError_t e = cudaSuccess;
+        if constexpr (NWC == 3 || NWC == 8) {
+            if (b->warps == 8) {
+                auto kern8 = batched_noflag_mixed_kernel<RG, NWC, 8>;
+                e = cudaFuncSetAttribute(kern8, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)b->smem);
+                if (e != cudaSuccess) return e;
+                b->grid = resident_blocks(kern8, b->smem, 256);
+            }
+        }
+        if (b->warps == 4) {
+            auto kern = batched_noflag_mixed_kernel<RG, NWC>;
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)b->smem);
+            if (e != cudaSuccess) return e;
+            b->grid = resident_blocks(kern, b->smem);
+        }
         b->grid_flag = resident_blocks(batched_flag_mixed_kernel<NWC, 2>, 0);
     } else {
         constexpr int RN = NWC <= 4 ? 4 : 2;
@@ -503,8 +528,19 @@ cudaError_t launch_persistent(gpp_batch *b, int wave, cudaStream_t s) {
             e = cudaGetLastError();
         }
         if (e == cudaSuccess && nu > 0) {
-            batched_noflag_mixed_kernel<RG, NWC><<<std::min(nu, b->grid), kThreads, b->smem, s>>>(
-                b->d_probs, b->d_parts, b->d_splits, b->d_items + w.i_mid, nu, heads + 1);
+            bool done = false;
+            if constexpr (NWC == 3 || NWC == 8) {
+                if (b->warps == 8) {
+                    batched_noflag_mixed_kernel<RG, NWC, 8><<<std::min(nu, b->grid), 256, b->smem,
+                                                              s>>>(
+                        b->d_probs, b->d_parts, b->d_splits, b->d_items + w.i_mid, nu, heads + 1);
+                    done = true;
+                }
+            }
+            if (!done)
+                batched_noflag_mixed_kernel<RG, NWC><<<std::min(nu, b->grid), kThreads, b->smem,
+                                                       s>>>(
+                    b->d_probs, b->d_parts, b->d_splits, b->d_items + w.i_mid, nu, heads + 1);
             e = cudaGetLastError();
         }
     } else {

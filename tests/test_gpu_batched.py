@@ -98,3 +98,31 @@ def test_batch_rejects_mixed_nw():
     probs, outs, keep = _arrays(devs + devs2, "fp64", with_n1=False)
     st = lib.gpp_sigma_batched(probs, outs, 3, None)
     assert st == capi.GPP_ERR_UNSUPPORTED
+
+
+def test_batch_follows_the_tuned_tile_shape():
+    """With an 8-bands-per-block variant chosen for 3 frequencies (as
+    gpp_autotune or gpp_set_variant would), the persistent kernel runs that
+    tile shape too: every state's bits equal its one-state call under the
+    same choice, and differ from the default shape's only by rounding."""
+    from gppsigma import ops
+    lib = capi.load()
+    names = ops.variant_names()
+    v8 = next(i for i, n in enumerate(names) if n.startswith("8 bands x 2 rows (8 warps)"))
+    devs = _states()
+    stream = torch.cuda.current_stream().cuda_stream
+    try:
+        capi.check(lib.gpp_set_variant(3, v8), "gpp_set_variant")
+        probs, outs, keep = _arrays(devs, "mixed", with_n1=False)
+        capi.check(lib.gpp_sigma_batched(probs, outs, len(devs), stream), "gpp_sigma_batched")
+        for d, (a, x, _) in zip(devs, keep):
+            ref = ops.sigma(d, "mixed")
+            ops.wait()
+            assert torch.equal(torch.view_as_real(a), torch.view_as_real(ref.achtemp))
+            assert torch.equal(torch.view_as_real(x), torch.view_as_real(ref.asxtemp))
+    finally:
+        ops.set_variant(3, -1)
+    for d, (a, x, _) in zip(devs, keep):
+        base = ops.sigma(d, "mixed")
+        ops.wait()
+        assert rel_err(a.cpu().numpy(), base.achtemp.cpu().numpy()) <= 1e-10
