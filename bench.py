@@ -533,8 +533,9 @@ def main() -> int:
                                     "unit": "TFLOP/s", "frac": a64 * 1e-12 / fp64_peak,
                                     "kernel": "noflag_fp64_kernel"}
 
-    # End to end through the host-buffer C-ABI call: pinned host inputs,
-    # H2D + kernels + D2H every step.
+    # End to end through the host-buffer C-ABI call: pinned host inputs
+    # (which the library pulls with a kernel on the SMs, overlapped with the
+    # computation), H2D + kernels + D2H every step.
     arrays = {}
     for k in ("aqsmtemp", "aqsntemp", "I_eps_array", "wtilde_array", "vcoul", "inv_igp_index",
               "indinv", "wx_array"):
