@@ -32,6 +32,7 @@
 // time.  Each output sums its k range in increasing k in one thread, and
 // split-k partials are added in split order: the results are bit-reproducible.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 
 #include "gpp_gemm.h"
@@ -162,15 +163,17 @@ template <bool XKFast, bool YKFast>
 cudaError_t launch_zgemm3m(const double2 *X, long long xs, const double2 *Y, long long ys,
                            double2 *Out, long long out_ld, long long split_stride, int M, int N,
                            int K, int splits, cudaStream_t s) {
-    static bool configured[256] = {};  // the attribute is set per device
+    // The shared-memory opt-in is set once per device (host threads may race
+    // to set it; setting it twice is harmless).
+    static std::atomic<bool> configured[256] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (!configured[dev & 255]) {
+    if (!configured[dev & 255].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(zgemm3m_kernel<XKFast, YKFast>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
         if (e != cudaSuccess) return e;
-        configured[dev & 255] = true;
+        configured[dev & 255].store(true, std::memory_order_release);
     }
     const int per = zgemm_k_per_split(K, splits);
     const int z = ceil_div(K, per);
