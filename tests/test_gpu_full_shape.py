@@ -83,3 +83,31 @@ def test_full_production_shape_matches_reference(case):
     print(case["name"], json.dumps(errs))
     del d
     torch.cuda.empty_cache()
+
+
+def test_full_production_shape_band_independent_gemm_paths():
+    """The production shape with one wx row for every band (the reference's
+    wx_array[3], so every drop-in entry point's case): the FP64 band-sum GEMM
+    path agrees with the per-term FP64 kernel within 1e-12, the mixed
+    float-float GEMM path with FP64 within 1e-10, per component, and the
+    per-band outputs likewise (norm-wise)."""
+    from gppsigma import ops as o
+    lib = capi.load()
+    d = o.device_inputs(W.CONFIGS["production"], 20240607)
+    d.wx_array = d.wx_array[:1].contiguous()
+    d.wx_stride = 0
+    res = {}
+    try:
+        for label, precision, mode in (("perterm", "fp64", 0), ("gemm", "fp64", 1),
+                                       ("mixed_gemm", "mixed", 1)):
+            capi.check(lib.gpp_set_gemm_path(mode), "gpp_set_gemm_path")
+            r = o.sigma(d, precision, acht_n1=True)
+            o.wait()
+            res[label] = {k: getattr(r, k).cpu().numpy() for k in ("achtemp", "asxtemp", "acht_n1_loc")}
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gpp_set_gemm_path")
+    ref = res["perterm"]
+    for label, tol in (("gemm", FP64_TOL), ("mixed_gemm", MIXED_DELIVERED)):
+        for k in ("achtemp", "asxtemp"):
+            assert rel_err(res[label][k], ref[k]) <= tol, (label, k)
+        assert norm_err(res[label]["acht_n1_loc"], ref["acht_n1_loc"]) <= tol, label
