@@ -54,6 +54,18 @@ flag_fp64_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
                                           (long long)blockIdx.y * row_tiles + row_tile, red, S);
 }
 
+// Band-independent frequencies: blockIdx.y covers NB occupied bands.
+template <int RG, int NWC, int NB, int THREADS, int SEM>
+__global__ void __launch_bounds__(THREADS)
+flag_fp64_multi_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
+    constexpr int K = NB * RG * NWC * 4;
+    __shared__ double red[(THREADS / 32) * K];
+    __shared__ double S[K];
+    flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + blockIdx.x,
+                                                    blockIdx.y * NB, blockIdx.z, row_tiles, red,
+                                                    S);
+}
+
 // Static term of reduce_achstemp (gppComplex_seq.cpp:66-101): one thread per
 // (n1, my_igp) pair; each block leaves one partial.
 __global__ void __launch_bounds__(256) achstemp_kernel(Problem p, double2 *partials, int *err) {
@@ -121,11 +133,37 @@ cudaError_t launch_noflag_t(const Problem &p, const Partials &part, int b0, int 
     return cudaGetLastError();
 }
 
+// Occupied bands in pairs when the frequencies are band-independent (the
+// solver once per pair; the same bits).  GPP_FLAG_MULTI=0 keeps one band per
+// block, read on every call.
+bool flag_multi_enabled() {
+    const char *v = getenv("GPP_FLAG_MULTI");
+    return !(v && v[0] == '0');
+}
+
+template <int RG, int NWC, int NB, int THREADS>
+cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles r, int row_tiles,
+                                cudaStream_t s) {
+    dim3 grid(r.end - r.begin, ceil_div(p.nv, NB), ceil_div(p.nw, NWC));
+    if (p.semantics == kSemKerSeq)
+        flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(
+            p, part, r.begin, row_tiles);
+    else
+        flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(
+            p, part, r.begin, row_tiles);
+    count_launch();
+    return cudaGetLastError();
+}
+
 template <int RG, int NWC, int THREADS>
 cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, cudaStream_t s) {
     const int row_tiles = ceil_div(p.ng, RG);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
+    if constexpr (NWC <= 4) {  // two bands of 8 frequencies would spill
+        if (p.wx_stride == 0 && p.nv >= 2 && flag_multi_enabled())
+            return launch_flag_multi_t<RG, NWC, 2, THREADS>(p, part, r, row_tiles, s);
+    }
     dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
     if (p.semantics == kSemKerSeq)
         flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(p, part, r.begin,

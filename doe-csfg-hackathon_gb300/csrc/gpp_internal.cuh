@@ -97,6 +97,30 @@ __device__ __forceinline__ double2 cscale(double2 a, double s) {
     return make_double2(a.x * s, a.y * s);
 }
 
+// The same complex operations with every rounding written out: __fma_rn,
+// __dmul_rn and __dadd_rn are never contracted or reassociated, so code built
+// from them gives the same bits in every kernel that inlines it, whatever
+// the compiler would fuse around a plain a*b + c in each instantiation.
+__device__ __forceinline__ double2 cmul_rn(double2 a, double2 b) {
+    return make_double2(__fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y)),
+                        __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ double2 cmul_conj_b_rn(double2 a, double2 b) {  // a * conj(b)
+    return make_double2(__fma_rn(a.x, b.x, __dmul_rn(a.y, b.y)),
+                        __fma_rn(a.y, b.x, -__dmul_rn(a.x, b.y)));
+}
+__device__ __forceinline__ double2 cscale_rn(double2 a, double s) {
+    return make_double2(__dmul_rn(a.x, s), __dmul_rn(a.y, s));
+}
+__device__ __forceinline__ double abs2_rn(double2 a) {
+    return __fma_rn(a.x, a.x, __dmul_rn(a.y, a.y));
+}
+// acc + a*b in two FMAs per component.
+__device__ __forceinline__ double2 cmul_acc_rn(double2 acc, double2 a, double2 b) {
+    return make_double2(__fma_rn(a.x, b.x, __fma_rn(-a.y, b.y, acc.x)),
+                        __fma_rn(a.x, b.y, __fma_rn(a.y, b.x, acc.y)));
+}
+
 // FP64 reciprocal: hardware seed (rcp.approx.ftz.f64, issued to the
 // multi-function unit, not the FP64 pipe) refined by one cubic Newton-Raphson
 // step r = r0 (1 + e + e^2), e = 1 - d r0 (the classical Newton iteration for

@@ -145,9 +145,12 @@ __device__ __forceinline__ void flag_epilogue(const Problem &p, const Partials &
                 if (igp < 0) continue;
                 const double2 m = __ldg(p.aqsm + (size_t)band * nc + igp);
                 const int k = (g * NWC + w) * 4 + (do_asx ? 2 : 0);
-                const double2 s = cmul(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
+                const double2 s =
+                    cmul_rn(make_double2(m.x, -m.y), make_double2(S[k], S[k + 1]));
                 const double v_igp = __ldg(p.vcoul + igp);
-                tot = cadd(tot, do_asx ? cscale(s, p.occ * v_igp) : cscale(cscale(s, 0.5), v_igp));
+                const double2 t = do_asx ? cscale_rn(s, __dmul_rn(p.occ, v_igp))
+                                         : cscale_rn(cscale_rn(s, 0.5), v_igp);
+                tot = make_double2(__dadd_rn(tot.x, t.x), __dadd_rn(tot.y, t.y));
             }
             if (do_ach)
                 part.ach[(long long)(iw0 + w) * part.ach_seg + part.ach_tile0 + tile] = tot;
@@ -159,33 +162,55 @@ __device__ __forceinline__ void flag_epilogue(const Problem &p, const Partials &
     }
 }
 
-// One occupied-band term of ssxt_scht_solver (gppComplex_seq.cpp:16-63),
-// accumulated as aqsn*sch and aqsn*ssx (the conj(aqsm) factor of
-// matngmatmgp is applied in the epilogue).  cwr = 1/wx^2 for branch A.
+// Per (row, column) factors of the occupied-band solver: wtilde^2 and
+// Omega2 = wtilde^2 I_eps (gppComplex_seq.cpp:346-350).
+__device__ __forceinline__ void flag_row_terms(double2 wt, double2 ie, double2 &wt2,
+                                               double2 &om2) {
+    wt2 = make_double2(__fma_rn(wt.x, wt.x, -__dmul_rn(wt.y, wt.y)),
+                       __dmul_rn(__dmul_rn(2.0, wt.x), wt.y));
+    om2 = cmul_rn(wt2, ie);
+}
+
+// ssxt_scht_solver (gppComplex_seq.cpp:16-63) for one (row, column,
+// frequency): sch and ssx before the aqsn factor.  cwr = 1/wx^2 for branch A.
+// Every rounding is explicit (the _rn helpers), so the one-band and the
+// band-pair tiles produce the same bits.
+template <int SEM>
+__device__ __forceinline__ void flag_solve(double wx, double cwr, double2 wt, double2 wt2,
+                                           double2 om2, double2 ie, double2 &sch_out,
+                                           double2 &ssx_out) {
+    const double2 wd = make_double2(__dsub_rn(wx, wt.x), -wt.y);
+    const double wdr = abs2_rn(wd);
+    const double rden = rcp_fp64(wdr);
+    const double2 delw = cscale_rn(cmul_conj_b_rn(wt, wd), rden);
+    const double delwr = abs2_rn(delw);
+    double2 sch = make_double2(0.0, 0.0), ssx = make_double2(0.0, 0.0);
+    if (wdr > kLimitTwo && delwr < kLimitOne) {
+        sch = cmul_rn(delw, ie);
+        ssx = cscale_rn(om2, cwr);
+    } else if (delwr > kTo1) {
+        const double2 cden =
+            cscale_rn(cmul_rn(wt2, make_double2(__dadd_rn(0.5, delw.x), delw.y)), 4.0);
+        const double r2 = rcp_fp64(abs2_rn(cden));
+        ssx = cmul_rn(cmul_conj_b_rn(make_double2(-om2.x, -om2.y), cden), cscale_rn(delw, r2));
+    }
+    // |ssx| > sexcut |I_eps| compared on squares (sexcut^2 = 16 is exact).
+    if (SEM == kSemComplexSeq && wx < 0.0 && abs2_rn(ssx) > __dmul_rn(16.0, abs2_rn(ie)))
+        ssx = make_double2(0.0, 0.0);
+    sch_out = sch;
+    ssx_out = ssx;
+}
+
+// One occupied-band term, accumulated as aqsn*sch and aqsn*ssx (the
+// conj(aqsm) factor of matngmatmgp is applied in the epilogue).
 template <int SEM>
 __device__ __forceinline__ void flag_term(double wx, double cwr, double2 wt, double2 wt2,
                                           double2 om2, double2 ie, double2 a, double2 &acc_s,
                                           double2 &acc_x) {
-    const double2 wd = make_double2(wx - wt.x, -wt.y);
-    const double wdr = wd.x * wd.x + wd.y * wd.y;
-    const double rden = rcp_fp64(wdr);
-    const double2 delw = cscale(cmul_conj_b(wt, wd), rden);
-    const double delwr = delw.x * delw.x + delw.y * delw.y;
-    double2 sch = make_double2(0.0, 0.0), ssx = make_double2(0.0, 0.0);
-    if (wdr > kLimitTwo && delwr < kLimitOne) {
-        sch = cmul(delw, ie);
-        ssx = cscale(om2, cwr);
-    } else if (delwr > kTo1) {
-        const double2 cden = cscale(cmul(wt2, make_double2(0.5 + delw.x, delw.y)), 4.0);
-        const double r2 = rcp_fp64(cden.x * cden.x + cden.y * cden.y);
-        ssx = cmul(cmul_conj_b(make_double2(-om2.x, -om2.y), cden), cscale(delw, r2));
-    }
-    // |ssx| > sexcut |I_eps| compared on squares (sexcut^2 = 16 is exact).
-    if (SEM == kSemComplexSeq && wx < 0.0 &&
-        ssx.x * ssx.x + ssx.y * ssx.y > 16.0 * (ie.x * ie.x + ie.y * ie.y))
-        ssx = make_double2(0.0, 0.0);
-    acc_s = cadd(acc_s, cmul(a, sch));
-    acc_x = cadd(acc_x, cmul(a, ssx));
+    double2 sch, ssx;
+    flag_solve<SEM>(wx, cwr, wt, wt2, om2, ie, sch, ssx);
+    acc_s = cmul_acc_rn(acc_s, a, sch);
+    acc_x = cmul_acc_rn(acc_x, a, ssx);
 }
 
 // One occupied-band tile in FP64: rows row_tile*RG.., one band, frequencies
@@ -232,8 +257,8 @@ __device__ __forceinline__ void flag_fp64_tile(const Problem &p, const Partials 
         for (int g = 0; g < RG; ++g) {
             const double2 wt = __ldg(wrow[g] + ig);
             const double2 ie = __ldg(erow[g] + ig);
-            const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
-            const double2 om2 = cmul(wt2, ie);
+            double2 wt2, om2;
+            flag_row_terms(wt, ie, wt2, om2);
 #pragma unroll
             for (int w = 0; w < NWC; ++w)
                 flag_term<SEM>(wx[w], cwr[w], wt, wt2, om2, ie, a, acc_s[g][w], acc_x[g][w]);
@@ -253,6 +278,96 @@ __device__ __forceinline__ void flag_fp64_tile(const Problem &p, const Partials 
         }
     block_reduce<K, THREADS>(v, red, S);
     flag_epilogue<RG, NWC>(p, part, S, row0, band, iw0, tile, row_tile);
+}
+
+// Occupied bands with band-independent frequencies (wx_stride == 0): the
+// solver's sch / ssx depend on (row, column, frequency) only, so one tile
+// evaluates them once for NB bands [band0, band0 + NB) and accumulates
+// aqsn * sch, aqsn * ssx per band.  Per band the operations, their order and
+// the reduction tree are those of flag_fp64_tile: the same bits, with 1/NB
+// of the solver work.  Bands past nv (a ragged last group) are computed on a
+// clamped band and not written.
+template <int RG, int NWC, int NB, int THREADS, int SEM>
+__device__ __forceinline__ void flag_fp64_multi_tile(const Problem &p, const Partials &part,
+                                                     int row_tile, int band0, int iw_chunk,
+                                                     int row_tiles, double *red, double *S) {
+    constexpr int KB = RG * NWC * 4, K = NB * KB;
+    const int row0 = row_tile * RG;
+    const int iw0 = iw_chunk * NWC;
+    const int nc = p.nc;
+
+    const double2 *wrow[RG];
+    const double2 *erow[RG];
+#pragma unroll
+    for (int g = 0; g < RG; ++g) {
+        const int r = min(row0 + g, p.ng - 1);
+        wrow[g] = p.wt + (size_t)r * nc;
+        erow[g] = p.ieps + (size_t)r * nc;
+    }
+    const double2 *nrow[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) nrow[b] = p.aqsn + (size_t)min(band0 + b, p.nv - 1) * nc;
+    double wx[NWC], cwr[NWC];
+#pragma unroll
+    for (int w = 0; w < NWC; ++w) {
+        wx[w] = __ldg(p.wx + min(iw0 + w, p.nw - 1));  // the same for every band
+        const double c = wx[w] * wx[w];
+        cwr[w] = c / (c * c);
+    }
+
+    double2 acc_s[NB][RG][NWC], acc_x[NB][RG][NWC];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                acc_s[b][g][w] = make_double2(0.0, 0.0);
+                acc_x[b][g][w] = make_double2(0.0, 0.0);
+            }
+
+    for (int ig = threadIdx.x; ig < nc; ig += THREADS) {
+        double2 a[NB];
+#pragma unroll
+        for (int b = 0; b < NB; ++b) a[b] = __ldg(nrow[b] + ig);
+#pragma unroll
+        for (int g = 0; g < RG; ++g) {
+            const double2 wt = __ldg(wrow[g] + ig);
+            const double2 ie = __ldg(erow[g] + ig);
+            double2 wt2, om2;
+            flag_row_terms(wt, ie, wt2, om2);
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                double2 sch, ssx;
+                flag_solve<SEM>(wx[w], cwr[w], wt, wt2, om2, ie, sch, ssx);
+#pragma unroll
+                for (int b = 0; b < NB; ++b) {
+                    acc_s[b][g][w] = cmul_acc_rn(acc_s[b][g][w], a[b], sch);
+                    acc_x[b][g][w] = cmul_acc_rn(acc_x[b][g][w], a[b], ssx);
+                }
+            }
+        }
+    }
+
+    double v[K];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+#pragma unroll
+        for (int g = 0; g < RG; ++g)
+#pragma unroll
+            for (int w = 0; w < NWC; ++w) {
+                const int k = b * KB + (g * NWC + w) * 4;
+                v[k] = acc_s[b][g][w].x;
+                v[k + 1] = acc_s[b][g][w].y;
+                v[k + 2] = acc_x[b][g][w].x;
+                v[k + 3] = acc_x[b][g][w].y;
+            }
+    block_reduce<K, THREADS>(v, red, S);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+        if (band0 + b < p.nv)
+            flag_epilogue<RG, NWC>(p, part, S + b * KB, row0, band0 + b, iw0,
+                                   (long long)(band0 + b) * row_tiles + row_tile, row_tile);
 }
 
 }  // namespace gpp

@@ -463,9 +463,10 @@ static __device__ __noinline__ FlagPole flag_pole(const Problem &p, int row, int
     const double2 wt = __ldg(p.wt + (size_t)row * nc + ig);
     const double2 ie = __ldg(p.ieps + (size_t)row * nc + ig);
     const double2 a = __ldg(p.aqsn + (size_t)band * nc + ig);
-    const double2 wt2 = make_double2(wt.x * wt.x - wt.y * wt.y, 2.0 * wt.x * wt.y);
+    double2 wt2, om2;
+    flag_row_terms(wt, ie, wt2, om2);
     double2 s64 = make_double2(0.0, 0.0), x64 = make_double2(0.0, 0.0);
-    flag_term<SEM>(wx, cwr, wt, wt2, cmul(wt2, ie), ie, a, s64, x64);
+    flag_term<SEM>(wx, cwr, wt, wt2, om2, ie, a, s64, x64);
     return {split(s64.x), split(s64.y), split(x64.x), split(x64.y)};
 }
 

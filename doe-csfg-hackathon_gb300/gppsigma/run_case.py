@@ -35,6 +35,8 @@ def main() -> int:
     ap.add_argument("--seed", type=int, default=20240607)
     ap.add_argument("--band-independent", action="store_true",
                     help="one wx row for every band (the reference's wx_array[3])")
+    ap.add_argument("--acht-n1", action="store_true",
+                    help="also produce the per-band output acht_n1_loc")
     args = ap.parse_args()
 
     import torch
@@ -50,7 +52,7 @@ def main() -> int:
     out = None
     for i in range(args.repeat):
         t0 = time.perf_counter()
-        out = ops.sigma(d, args.precision, args.semantics, out=out)
+        out = ops.sigma(d, args.precision, args.semantics, out=out, acht_n1=args.acht_n1)
         ops.wait()
         dt = time.perf_counter() - t0
         print(f"step {i}: {dt * 1e3:.2f} ms, {shape.terms / dt:.4e} terms/s")

@@ -2,6 +2,8 @@
 the same sums as the per-term kernel and the oracle (achtemp, asxtemp,
 acht_n1_loc, the static term), on ragged shapes, clamped G' indices,
 near-pole wtilde, every frequency-chunk width and the overlapped host path."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -164,3 +166,34 @@ def test_mixed_gemm_path_through_the_host_pieces():
     assert np.array_equal(host["achtemp"], dev.achtemp.cpu().numpy())
     assert np.array_equal(host["asxtemp"], dev.asxtemp.cpu().numpy())
     assert np.array_equal(host["acht_n1_loc"], dev.acht_n1_loc.cpu().numpy())
+
+
+@pytest.mark.parametrize("shape,semantics", [
+    (W.Shape(40, 2, 777, 13, 3, near_pole=0.05), "complex_seq"),
+    (W.Shape(33, 5, 640, 8, 4, igp_overflow=2), "kerseq"),
+    (W.Shape(20, 3, 300, 9, 1), "complex_seq"),
+    (W.Shape(16, 4, 513, 7, 2, near_pole=0.05), "kerseq"),
+    (W.Shape(12, 1, 400, 5, 3), "complex_seq"),
+    (W.Shape(24, 7, 256, 3, 8, dw=0.25), "complex_seq"),
+])
+def test_occupied_band_pairs_give_the_per_band_bits(shape, semantics, monkeypatch):
+    """With one wx row for every band the FP64 occupied-band kernel solves
+    each (row, column, frequency) once for a pair of bands.  Its sums must be
+    the bits of one band per block: the same call with GPP_FLAG_MULTI=0, and
+    the same wx replicated into one row per band (the per-band kernel)."""
+    from gppsigma import ops
+    inp = band_independent(shape, 23)
+    rep = dataclasses.replace(inp, wx_array=np.repeat(inp.wx_array, shape.number_bands, axis=0))
+    d = ops.DeviceInputs.from_host(inp)
+    d_rep = ops.DeviceInputs.from_host(rep)
+    assert d.wx_stride == 0 and d_rep.wx_stride == shape.nw
+    n1 = shape.nw >= 3
+    pair = sigma_with(0, d, semantics, n1)
+    replicated = sigma_with(0, d_rep, semantics, n1)
+    monkeypatch.setenv("GPP_FLAG_MULTI", "0")
+    single = sigma_with(0, d, semantics, n1)
+    keys = ("achtemp", "asxtemp") + (("acht_n1_loc",) if n1 else ())
+    for key in keys:
+        a = getattr(pair, key).cpu().numpy()
+        assert np.array_equal(a, getattr(single, key).cpu().numpy()), key
+        assert np.array_equal(a, getattr(replicated, key).cpu().numpy()), key
