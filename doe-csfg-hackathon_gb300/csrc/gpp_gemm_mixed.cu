@@ -4,12 +4,15 @@
 // same factorisation, and its derivation, is gpp_gemm.cu).
 //
 // The GEMM keeps the packed layout of the mixed kernels: a thread owns one
-// G' row pair -- the two lanes of every f32x2 instruction -- and 8 columns,
-// so one complex float-float multiply-add of both rows is 48 packed
-// instructions (4 products, 4 TwoSum-based additions).  A block computes 16
-// row pairs x 128 columns, staging 16 bands of c and aqsn per step in shared
-// memory.  G is written as row-pair planes like wtilde and Q, and the
-// frequency pass reads it exactly as the per-term kernel reads aqsn * Q:
+// G' row pair -- the two lanes of every f32x2 instruction -- and 8 columns.
+// Complex products take Gauss's 3M form with three float-float accumulators
+// per output (ar br, ai bi, (ar + ai)(br + bi)), so one complex multiply-add
+// of both rows is 36 packed instructions (3 products, 3 TwoSum-based
+// additions) instead of 48; the sums re + im are formed once per staged
+// element.  A block computes 8 row pairs x 128 columns, staging 8 bands of
+// c and aqsn per step in shared memory.  G is written as row-pair planes like
+// wtilde and Q, and the frequency pass reads it exactly as the per-term
+// kernel reads aqsn * Q:
 // terms within 1e-3 |wx| of the pole are recomputed in FP64 from the inputs
 // and G.  Compared with the per-term kernel the division runs once per
 // (row, column, frequency) instead of once per band.  The per-band output
@@ -25,10 +28,20 @@ gpp_status set_error(gpp_status s, const char *msg);
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kPairs = 16;   // row pairs per GEMM block
-constexpr int kCols = 128;   // columns per GEMM block
-constexpr int kStep = 16;    // bands per shared-memory step
-constexpr int kPerThread = kCols / (kThreads / kPairs);  // columns per thread (8)
+// The two float-float GEMMs: 128 threads, 8 row pairs per block, so 16
+// threads per row pair, each owning kPerThread columns (G) or bands (H) with
+// three df accumulators apiece; kStep k values per shared-memory step.
+// Shapes and resident blocks as measured fastest on the GB300 at the
+// production shape among 8 x 128 / 8 x 64 / 4 x 128 tiles at 3-5 blocks per
+// SM: G 8 x 128 at 3 blocks (168 registers), H 8 x 64 at 5 (at most 102).
+constexpr int kGemmThreads = 128;
+constexpr int kPairs = 8;      // row pairs per GEMM block
+constexpr int kLanes = kGemmThreads / kPairs;  // threads per row pair (16)
+constexpr int kStep = 8;       // k values per shared-memory step
+constexpr int kCols = 128;     // G: columns per block
+constexpr int kGMinBlocks = 3;
+constexpr int kHBands = 64;    // H: bands per block
+constexpr int kHMinBlocks = 5;
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 int row_pairs(const Problem &p) { return (p.ng + 1) / 2; }
@@ -68,62 +81,106 @@ __global__ void __launch_bounds__(kThreads) mg_coeff_kernel(Problem p, int b0, i
     }
 }
 
+// One k step of the 3M (Gauss) float-float complex multiply-add for kPer
+// outputs: a = ar + i ai (the row pair's lanes, sa = ar + ai) times
+// b = br + i bi (broadcast, sb = br + bi).  P1 = ar br, P2 = ai bi and
+// P3 = sa sb accumulate separately; the product sum is P1 - P2 + i (P3 - P1
+// - P2), formed once at the end (mg_3m_result).  Three df products and three
+// df sums per output and k -- 36 packed instructions, against 48 for the
+// four products and four sums of the direct form.
+template <int PER>
+__device__ __forceinline__ void mg_3m_step(const float4 a4, const float4 b4, const float4 s4,
+                                           const float4 *bv, const float2 *sv, int stride,
+                                           df2 (&acc)[3][PER]) {
+    const df2 ar = {f2(a4.x, a4.y), f2(a4.z, a4.w)};
+    const df2 ai = {f2(b4.x, b4.y), f2(b4.z, b4.w)};
+    const df2 sa = {f2(s4.x, s4.y), f2(s4.z, s4.w)};
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const float4 v = bv[t * stride];
+        const float2 w = sv[t * stride];
+        acc[0][t] = df2_add(acc[0][t], df2_mul(ar, df2_bcast(df{v.x, v.y})));
+        acc[1][t] = df2_add(acc[1][t], df2_mul(ai, df2_bcast(df{v.z, v.w})));
+        acc[2][t] = df2_add(acc[2][t], df2_mul(sa, df2_bcast(df{w.x, w.y})));
+    }
+}
+
+// Real and imaginary parts from the three sums, renormalised (the
+// imaginary part can cancel), as two float4 (hi r0, hi r1, lo r0, lo r1).
+__device__ __forceinline__ void mg_3m_result(const df2 &p1, const df2 &p2, const df2 &p3,
+                                             float4 &re, float4 &im) {
+    const df2 r = df2_norm(df2_sub(p1, p2));
+    const df2 i = df2_norm(df2_sub(df2_sub(p3, p1), p2));
+    re = make_float4(r.h.x, r.h.y, r.l.x, r.l.y);
+    im = make_float4(i.h.x, i.h.y, i.l.x, i.l.y);
+}
+
+// Staging of the 3M operands: the row pair's (re, im, re + im) and the
+// broadcast operand's (re, im) float4 with its re + im as a float2; the
+// sums are renormalised df values, formed once per staged element.
+__device__ __forceinline__ void mg_stage_a(float4 re, float4 im, float4 *dst) {
+    const df2 s = df2_norm(df2_add(df2{f2(re.x, re.y), f2(re.z, re.w)},
+                                   df2{f2(im.x, im.y), f2(im.z, im.w)}));
+    dst[0] = re;
+    dst[1] = im;
+    dst[2] = make_float4(s.h.x, s.h.y, s.l.x, s.l.y);
+}
+__device__ __forceinline__ void mg_stage_b(float4 v, float4 *dst, float2 *sum) {
+    const df s = df_norm(df_add(df{v.x, v.y}, df{v.z, v.w}));
+    *dst = v;
+    *sum = make_float2(s.h, s.l);
+}
+
 // G[j][col] = sum_k c[k][j] aqsn[k][col] in float-float, both rows of pair j
 // as the lanes.  Grid: x over blocks of kPairs row pairs (fastest, so blocks
 // in flight share their aqsn columns in L2), y over blocks of kCols columns.
-__global__ void __launch_bounds__(kThreads, 2) mg_gemm_kernel(int K, int pairs, int nc,
-                                                              const float4 *__restrict__ cpl,
-                                                              const float4 *__restrict__ band,
-                                                              float4 *__restrict__ G) {
-    __shared__ float4 sA[kStep][kPairs][2];
+__global__ void __launch_bounds__(kGemmThreads, kGMinBlocks) mg_gemm_kernel(
+    int K, int pairs, int nc, const float4 *__restrict__ cpl, const float4 *__restrict__ band,
+    float4 *__restrict__ G) {
+    __shared__ float4 sA[kStep][kPairs][3];
     __shared__ float4 sB[kStep][kCols];
+    __shared__ float2 sS[kStep][kCols];
+    constexpr int kPerThread = kCols / kLanes;
     const int tid = threadIdx.x;
-    const int pr = tid / (kThreads / kPairs), cg = tid % (kThreads / kPairs);
+    const int pr = tid / kLanes, cg = tid % kLanes;
     const int pair0 = blockIdx.x * kPairs, col0 = blockIdx.y * kCols;
     const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
-    df2 accr[kPerThread], acci[kPerThread];
+    df2 acc[3][kPerThread];
 #pragma unroll
-    for (int t = 0; t < kPerThread; ++t) accr[t] = acci[t] = z;
+    for (int t = 0; t < kPerThread; ++t) acc[0][t] = acc[1][t] = acc[2][t] = z;
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k0 = 0; k0 < K; k0 += kStep) {
         const int kc = min(kStep, K - k0);
         __syncthreads();  // the previous step's operands are consumed
-        for (int i = tid; i < kStep * kPairs * 2; i += kThreads) {
-            const int kk = i / (kPairs * 2), pp = (i / 2) % kPairs, c = i % 2;
-            float4 v = zero4;
-            if (kk < kc && pair0 + pp < pairs)
-                v = cpl[((size_t)(k0 + kk) * pairs + pair0 + pp) * 2 + c];
-            sA[kk][pp][c] = v;
+        for (int i = tid; i < kStep * kPairs; i += kGemmThreads) {
+            const int kk = i / kPairs, pp = i % kPairs;
+            float4 re = zero4, im = zero4;
+            if (kk < kc && pair0 + pp < pairs) {
+                const float4 *c = cpl + ((size_t)(k0 + kk) * pairs + pair0 + pp) * 2;
+                re = c[0];
+                im = c[1];
+            }
+            mg_stage_a(re, im, sA[kk][pp]);
         }
-        for (int i = tid; i < kStep * kCols; i += kThreads) {
+        for (int i = tid; i < kStep * kCols; i += kGemmThreads) {
             const int kk = i / kCols, cc = i % kCols;
             float4 v = zero4;
             if (kk < kc && col0 + cc < nc) v = band[(size_t)(k0 + kk) * nc + col0 + cc];
-            sB[kk][cc] = v;
+            mg_stage_b(v, &sB[kk][cc], &sS[kk][cc]);
         }
         __syncthreads();
-        for (int kk = 0; kk < kc; ++kk) {
-            const float4 a4 = sA[kk][pr][0], b4 = sA[kk][pr][1];
-            const df2 ar = {f2(a4.x, a4.y), f2(a4.z, a4.w)};
-            const df2 ai = {f2(b4.x, b4.y), f2(b4.z, b4.w)};
-#pragma unroll
-            for (int t = 0; t < kPerThread; ++t) {
-                const float4 v = sB[kk][cg + t * (kThreads / kPairs)];
-                const df2 br = df2_bcast(df{v.x, v.y}), bi = df2_bcast(df{v.z, v.w});
-                accr[t] = df2_sub(df2_add(accr[t], df2_mul(ar, br)), df2_mul(ai, bi));
-                acci[t] = df2_add(df2_add(acci[t], df2_mul(ar, bi)), df2_mul(ai, br));
-            }
-        }
+        for (int kk = 0; kk < kc; ++kk)
+            mg_3m_step<kPerThread>(sA[kk][pr][0], sA[kk][pr][1], sA[kk][pr][2], &sB[kk][cg],
+                                   &sS[kk][cg], kLanes, acc);
     }
     const int j = pair0 + pr;
     if (j >= pairs) return;
 #pragma unroll
     for (int t = 0; t < kPerThread; ++t) {
-        const int col = col0 + cg + t * (kThreads / kPairs);
+        const int col = col0 + cg + t * kLanes;
         if (col >= nc) continue;
-        G[(size_t)j * 2 * nc + col] = make_float4(accr[t].h.x, accr[t].h.y, accr[t].l.x, accr[t].l.y);
-        G[(size_t)j * 2 * nc + nc + col] =
-            make_float4(acci[t].h.x, acci[t].h.y, acci[t].l.x, acci[t].l.y);
+        mg_3m_result(acc[0][t], acc[1][t], acc[2][t], G[(size_t)j * 2 * nc + col],
+                     G[(size_t)j * 2 * nc + nc + col]);
     }
 }
 
@@ -262,67 +319,59 @@ __global__ void __launch_bounds__(kThreads) mg_m2_kernel(Problem p, SplitPlanes 
     }
 }
 
-constexpr int kHBands = 128;   // bands per H block
 constexpr int kHChunks = 16;   // column chunks of the H sum (summed in order afterwards)
 
 // Hp[z][k][j] = sum over columns of chunk z of aqsn[k][ig] M_2[j][ig]:
 // both rows of pair j as the lanes, the band value broadcast.  Grid: x row
 // pair blocks, y band blocks, z column chunks.
-__global__ void __launch_bounds__(kThreads, 2) mg_gemm_h_kernel(int nbands, int pairs, int nc,
-                                                                int chunk,
-                                                                const float4 *__restrict__ M2,
-                                                                const float4 *__restrict__ band,
-                                                                float4 *__restrict__ Hp) {
-    __shared__ float4 sA[kStep][kPairs][2];
+__global__ void __launch_bounds__(kGemmThreads, kHMinBlocks) mg_gemm_h_kernel(
+    int nbands, int pairs, int nc, int chunk, const float4 *__restrict__ M2,
+    const float4 *__restrict__ band, float4 *__restrict__ Hp) {
+    __shared__ float4 sA[kStep][kPairs][3];
     __shared__ float4 sB[kStep][kHBands];
+    __shared__ float2 sS[kStep][kHBands];
+    constexpr int kPerThread = kHBands / kLanes;
     const int tid = threadIdx.x;
-    const int pr = tid / (kThreads / kPairs), cg = tid % (kThreads / kPairs);
+    const int pr = tid / kLanes, cg = tid % kLanes;
     const int pair0 = blockIdx.x * kPairs, band0 = blockIdx.y * kHBands;
     const int ig_begin = blockIdx.z * chunk, ig_end = min(nc, ig_begin + chunk);
     const df2 z = {f2(0.f, 0.f), f2(0.f, 0.f)};
-    df2 accr[kPerThread], acci[kPerThread];
+    df2 acc[3][kPerThread];
 #pragma unroll
-    for (int t = 0; t < kPerThread; ++t) accr[t] = acci[t] = z;
+    for (int t = 0; t < kPerThread; ++t) acc[0][t] = acc[1][t] = acc[2][t] = z;
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int ig0 = ig_begin; ig0 < ig_end; ig0 += kStep) {
         const int kc = min(kStep, ig_end - ig0);
         __syncthreads();
-        for (int i = tid; i < kStep * kPairs * 2; i += kThreads) {
-            const int pp = i / (kStep * 2), c = (i / kStep) % 2, kk = i % kStep;
-            float4 v = zero4;
-            if (kk < kc && pair0 + pp < pairs)
-                v = M2[((size_t)(pair0 + pp) * 2 + c) * nc + ig0 + kk];
-            sA[kk][pp][c] = v;
+        for (int i = tid; i < kStep * kPairs; i += kGemmThreads) {
+            const int pp = i / kStep, kk = i % kStep;
+            float4 re = zero4, im = zero4;
+            if (kk < kc && pair0 + pp < pairs) {
+                const float4 *m = M2 + (size_t)(pair0 + pp) * 2 * nc + ig0 + kk;
+                re = m[0];
+                im = m[nc];
+            }
+            mg_stage_a(re, im, sA[kk][pp]);
         }
-        for (int i = tid; i < kStep * kHBands; i += kThreads) {
+        for (int i = tid; i < kStep * kHBands; i += kGemmThreads) {
             const int bb = i / kStep, kk = i % kStep;
             float4 v = zero4;
             if (kk < kc && band0 + bb < nbands) v = band[(size_t)(band0 + bb) * nc + ig0 + kk];
-            sB[kk][bb] = v;
+            mg_stage_b(v, &sB[kk][bb], &sS[kk][bb]);
         }
         __syncthreads();
-        for (int kk = 0; kk < kc; ++kk) {
-            const float4 a4 = sA[kk][pr][0], b4 = sA[kk][pr][1];
-            const df2 ar = {f2(a4.x, a4.y), f2(a4.z, a4.w)};
-            const df2 ai = {f2(b4.x, b4.y), f2(b4.z, b4.w)};
-#pragma unroll
-            for (int t = 0; t < kPerThread; ++t) {
-                const float4 v = sB[kk][cg + t * (kThreads / kPairs)];
-                const df2 br = df2_bcast(df{v.x, v.y}), bi = df2_bcast(df{v.z, v.w});
-                accr[t] = df2_sub(df2_add(accr[t], df2_mul(ar, br)), df2_mul(ai, bi));
-                acci[t] = df2_add(df2_add(acci[t], df2_mul(ar, bi)), df2_mul(ai, br));
-            }
-        }
+        for (int kk = 0; kk < kc; ++kk)
+            mg_3m_step<kPerThread>(sA[kk][pr][0], sA[kk][pr][1], sA[kk][pr][2], &sB[kk][cg],
+                                   &sS[kk][cg], kLanes, acc);
     }
     const int j = pair0 + pr;
     if (j >= pairs) return;
 #pragma unroll
     for (int t = 0; t < kPerThread; ++t) {
-        const int k = band0 + cg + t * (kThreads / kPairs);
+        const int k = band0 + cg + t * kLanes;
         if (k >= nbands) continue;
         float4 *o = Hp + (((size_t)blockIdx.z * nbands + k) * pairs + j) * 2;
-        o[0] = make_float4(accr[t].h.x, accr[t].h.y, accr[t].l.x, accr[t].l.y);
-        o[1] = make_float4(acci[t].h.x, acci[t].h.y, acci[t].l.x, acci[t].l.y);
+        mg_3m_result(acc[0][t], acc[1][t], acc[2][t], o[0], o[1]);
     }
 }
 
@@ -401,7 +450,7 @@ gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *spl
     if (ceil_div(p.nc, kCols) > 65535)
         return set_error(GPP_ERR_UNSUPPORTED, "ncouls too large for the band-sum GEMM grid");
     dim3 grid((unsigned)ceil_div(pairs, kPairs), (unsigned)ceil_div(p.nc, kCols));
-    mg_gemm_kernel<<<grid, kThreads, 0, st>>>(K, pairs, p.nc, cpl, s.band + (size_t)b0 * p.nc,
+    mg_gemm_kernel<<<grid, kGemmThreads, 0, st>>>(K, pairs, p.nc, cpl, s.band + (size_t)b0 * p.nc,
                                               planes_g(p, ws, K));
     count_launch();
     e = cudaGetLastError();
@@ -445,7 +494,7 @@ gpp_status mixed_gemm_per_band(const Problem &p, const Partials &part, void *spl
     if (ceil_div(K, kHBands) > 65535)
         return set_error(GPP_ERR_UNSUPPORTED, "too many bands for the per-band product grid");
     dim3 grid((unsigned)ceil_div(pairs, kPairs), (unsigned)ceil_div(K, kHBands), (unsigned)chunks);
-    mg_gemm_h_kernel<<<grid, kThreads, 0, st>>>(K, pairs, p.nc, chunk, M2,
+    mg_gemm_h_kernel<<<grid, kGemmThreads, 0, st>>>(K, pairs, p.nc, chunk, M2,
                                                 s.band + (size_t)b0 * p.nc, Hp);
     count_launch();
     e = cudaGetLastError();
