@@ -24,13 +24,16 @@ thread_local std::string t_err;
 thread_local unsigned long long t_launches = 0;
 thread_local cudaStream_t t_compat_stream = nullptr;
 thread_local int t_dropin_precision = -1;  // -1: the process default
-thread_local int t_gemm_path = -1;         // -1: automatic, 0: never, 1: whenever it applies
+thread_local int t_gemm_path = -1;         // -1: automatic, 0: never, 1: whenever it applies,
+                                            // 2: as 1 with the FP64 GEMM on the FP64 pipe
 thread_local bool t_timing = false;
 thread_local cudaEvent_t t_ev0 = nullptr, t_ev1 = nullptr;
 thread_local bool t_timed = false;
 }  // namespace
 
 void count_launch(int n) { t_launches += (unsigned long long)n; }
+
+bool fp64_gemm_on_tensor_cores() { return t_gemm_path != 2; }
 
 // Records `msg` as this thread's gpp_last_error_message and returns `s`.
 gpp_status set_error(gpp_status s, const char *msg) {
@@ -199,7 +202,7 @@ int dropin_precision() {
 constexpr int kGemmMinBands = 32;
 bool gemm_path(int wx_stride, int bands) {
     if (wx_stride != 0 || bands <= 0) return false;
-    return t_gemm_path < 0 ? bands >= kGemmMinBands : t_gemm_path == 1;
+    return t_gemm_path < 0 ? bands >= kGemmMinBands : t_gemm_path >= 1;
 }
 
 // Whether the mixed path runs the occupied-band kernel concurrently on the
@@ -499,7 +502,7 @@ gpp_status gpp_set_stream(gpp_stream_t stream) {
 gpp_stream_t gpp_get_stream(void) { return reinterpret_cast<gpp_stream_t>(t_compat_stream); }
 
 gpp_status gpp_set_gemm_path(int mode) {
-    if (mode < -1 || mode > 1) return fail(GPP_ERR_INVALID_ARGUMENT, "gemm path mode %d", mode);
+    if (mode < -1 || mode > 2) return fail(GPP_ERR_INVALID_ARGUMENT, "gemm path mode %d", mode);
     t_gemm_path = mode;
     return GPP_OK;
 }

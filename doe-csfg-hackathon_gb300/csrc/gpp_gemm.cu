@@ -36,6 +36,7 @@
 #include <cstdio>
 
 #include "gpp_gemm.h"
+#include "gpp_ozaki.h"
 
 namespace gpp {
 
@@ -187,8 +188,12 @@ cudaError_t launch_zgemm3m(const double2 *X, long long xs, const double2 *Y, lon
 }
 
 // k splits of the per-band GEMM (H = aqsn M_2^T sums over all ncouls
-// columns): enough blocks for ~10 waves of two blocks per SM.
+// columns): on the FP64 pipe enough blocks for ~10 waves of two blocks per
+// SM; on the tensor cores (128 x 128 output tiles, so only 4 x 13 tiles at
+// the production shape) 32 splits make ~5 waves.
 constexpr int kHSplits = 8;
+constexpr int kHSplitsTensor = 32;
+int h_splits() { return fp64_gemm_on_tensor_cores() ? kHSplitsTensor : kHSplits; }
 
 // c[k][r] for bands b0 + k (k < K) and rows [r0, r1); rows whose G' index
 // is invalid get 0 (their fault bit is set, as in the per-term epilogue).
@@ -332,18 +337,27 @@ cudaError_t launch_epilogue_t(const Problem &p, const Partials &part, const doub
 
 }  // namespace
 
+// Scratch of the tensor-core GEMMs: G's, then (reused) H's.
+size_t ozaki_scratch(const Problem &p, int bands, bool want_n1) {
+    if (!fp64_gemm_on_tensor_cores()) return 0;
+    size_t b = ozaki_bytes(p.ng, p.nc, bands, 1);
+    if (want_n1) b = std::max(b, ozaki_bytes(bands, p.ng, p.nc, kHSplitsTensor));
+    return b;
+}
+
 size_t gemm_bytes(const Problem &p, int bands, bool want_n1) {
     const size_t k = (size_t)bands, ng = (size_t)p.ng, nc = (size_t)p.nc;
     size_t b = align_up(sizeof(double2) * k * ng) + align_up(sizeof(double2) * ng * nc);
     if (want_n1)
-        b += align_up(sizeof(double2) * ng * nc) + align_up(sizeof(double2) * kHSplits * k * ng);
-    return b;
+        b += align_up(sizeof(double2) * ng * nc) + align_up(sizeof(double2) * h_splits() * k * ng);
+    return b + align_up(ozaki_scratch(p, bands, want_n1));
 }
 
 namespace {
 
 struct GemmBuffers {
     double2 *C, *G, *M2, *H;
+    void *oz;  // tensor-core GEMM scratch
 };
 
 GemmBuffers carve(const Problem &p, void *ws, int K, bool want_n1) {
@@ -358,7 +372,9 @@ GemmBuffers carve(const Problem &p, void *ws, int K, bool want_n1) {
         b.M2 = reinterpret_cast<double2 *>(w);
         w += align_up(sizeof(double2) * ng * nc);
         b.H = reinterpret_cast<double2 *>(w);
+        w += align_up(sizeof(double2) * h_splits() * (size_t)K * ng);
     }
+    b.oz = w;
     return b;
 }
 
@@ -375,6 +391,12 @@ gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_coeff_kernel");
     // G (ng x nc) = C^T aqsn: X(r, k) = C[k][r], Y(ig, k) = aqsn[b0 + k][ig].
+    if (fp64_gemm_on_tensor_cores()) {
+        const OzOperand X{b.C, p.ng, false, p.ng}, Y{p.aqsn + (size_t)b0 * p.nc, p.nc, false, p.nc};
+        e = ozaki_zgemm(X, Y, p.ng, p.nc, K, 1, b.G, p.nc, 0, b.oz, s);
+        if (e != cudaSuccess) return cuda_fail(e, "ozaki_zgemm (band sum)");
+        return GPP_OK;
+    }
     e = launch_zgemm3m<false, false>(b.C, p.ng, p.aqsn + (size_t)b0 * p.nc, p.nc, b.G, p.nc, 0,
                                      p.ng, p.nc, K, 1, s);
     if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (band sum)");
@@ -408,14 +430,23 @@ gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
     // H (K x ng) = aqsn M_2^T: X(k', ig) = aqsn[b0 + k'][ig], Y(r, ig) = M_2[r][ig],
-    // the ncouls sum split kHSplits ways.
-    e = launch_zgemm3m<true, true>(p.aqsn + (size_t)b0 * p.nc, p.nc, b.M2, p.nc, b.H, p.ng,
-                                   (long long)K * p.ng, K, p.ng, p.nc, kHSplits, s);
-    if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (per-band output)");
+    // the ncouls sum split up to h_splits() ways.
+    int splits;
+    if (fp64_gemm_on_tensor_cores()) {
+        const OzOperand X{p.aqsn + (size_t)b0 * p.nc, p.nc, true, K}, Y{b.M2, p.nc, true, p.ng};
+        e = ozaki_zgemm(X, Y, K, p.ng, p.nc, kHSplitsTensor, b.H, p.ng, (long long)K * p.ng, b.oz,
+                        s);
+        if (e != cudaSuccess) return cuda_fail(e, "ozaki_zgemm (per-band output)");
+        splits = ozaki_splits(p.nc, kHSplitsTensor);
+    } else {
+        e = launch_zgemm3m<true, true>(p.aqsn + (size_t)b0 * p.nc, p.nc, b.M2, p.nc, b.H, p.ng,
+                                       (long long)K * p.ng, K, p.ng, p.nc, kHSplits, s);
+        if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (per-band output)");
+        splits = zgemm_splits(p.nc, kHSplits);
+    }
     const int tiles = ceil_div(p.ng, 2);
     gemm_n1_kernel<<<grid_for((long long)K * tiles), kThreads, 0, s>>>(p, part, b0, K, 0, tiles,
-                                                                       b.C, b.H,
-                                                                       zgemm_splits(p.nc, kHSplits));
+                                                                       b.C, b.H, splits);
     count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "gemm_n1_kernel");

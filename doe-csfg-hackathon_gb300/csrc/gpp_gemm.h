@@ -9,6 +9,11 @@
 
 namespace gpp {
 
+// Whether this host thread's FP64 GEMMs run on the tensor cores (the Ozaki
+// split of gpp_ozaki.cu, the default) rather than on the FP64 pipe
+// (zgemm3m_kernel, gpp_set_gemm_path(2)).
+bool fp64_gemm_on_tensor_cores();
+
 // Workspace bytes of the GEMM path for `bands` unoccupied bands.
 size_t gemm_bytes(const Problem &p, int bands, bool want_n1);
 

@@ -27,7 +27,7 @@ DRIVER = os.path.join(LIBDIR, "gpp_driver.ex")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 LIB_SOURCES = ["gpp_api.cu", "gpp_fp64.cu", "gpp_mixed.cu", "gpp_batched.cu", "gpp_static.cu",
-               "gpp_gemm.cu", "gpp_gemm_mixed.cu", "gpp_compat.cpp"]
+               "gpp_gemm.cu", "gpp_gemm_mixed.cu", "gpp_ozaki.cu", "gpp_compat.cpp"]
 DRIVER_SOURCES = ["gpp_driver.cpp"]
 
 

@@ -37,10 +37,13 @@ def main() -> int:
                     help="one wx row for every band (the reference's wx_array[3])")
     ap.add_argument("--acht-n1", action="store_true",
                     help="also produce the per-band output acht_n1_loc")
+    ap.add_argument("--gemm-path", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="gpp_set_gemm_path mode for band-independent wx (2: FP64 GEMMs on the "
+                         "FP64 pipe instead of the tensor cores)")
     args = ap.parse_args()
 
     import torch
-    from gppsigma import ops
+    from gppsigma import capi, ops
 
     torch.cuda.set_device(0)
     shape = SHAPES[args.workload]
@@ -49,6 +52,7 @@ def main() -> int:
         import dataclasses
         d = dataclasses.replace(d, wx_array=d.wx_array.reshape(-1, shape.nw)[:1].contiguous(),
                                 wx_stride=0)
+    capi.check(capi.load().gpp_set_gemm_path(args.gemm_path), "gpp_set_gemm_path")
     out = None
     for i in range(args.repeat):
         t0 = time.perf_counter()

@@ -144,12 +144,15 @@ int gpp_get_dropin_precision(void);
  * frequencies (wx_stride == 0: the drop-in entry points and gpp_sigma)
  * compute their unoccupied bands (per host thread): -1 (default) through
  * the band-sum GEMM when there are at least 32 unoccupied bands, 0 always
- * with the per-term kernel, 1 always through the GEMM.  With wx the same
+ * with the per-term kernel, 1 always through the GEMM, 2 as 1 with the FP64
+ * GEMMs on the FP64 pipe instead of the tensor cores.  With wx the same
  * for every band the band sum factors out of the division:
  * achtemp[iw] = sum_{G',ig} M_iw G, G = sum_n1 c aqsn (one complex GEMM,
- * written in this library: 3M-form FP64 on the FP64 pipe, float-float on the
- * FP32 pipes in mixed precision), several times faster; the results agree
- * with the per-term kernels to their rounding. */
+ * written in this library: in FP64 by default on the tensor cores, the
+ * operands split into bf16 integer slices whose products the tensor cores
+ * sum exactly (Ozaki scheme), with mode 2 as a 3M-form GEMM on the FP64
+ * pipe; float-float on the FP32 pipes in mixed precision), several times
+ * faster; the results agree with the per-term kernels to their rounding. */
 gpp_status gpp_set_gemm_path(int mode);
 
 /* ------------------------------------------------------------------------

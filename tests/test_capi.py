@@ -73,9 +73,9 @@ def test_invalid_arguments_are_reported_without_a_device(lib):
 
 
 def test_path_and_precision_setters_validate(lib):
-    assert lib.gpp_set_gemm_path(2) == capi.GPP_ERR_INVALID_ARGUMENT
+    assert lib.gpp_set_gemm_path(3) == capi.GPP_ERR_INVALID_ARGUMENT
     assert lib.gpp_set_gemm_path(-2) == capi.GPP_ERR_INVALID_ARGUMENT
-    for mode in (1, 0, -1):
+    for mode in (2, 1, 0, -1):
         assert lib.gpp_set_gemm_path(mode) == capi.GPP_OK
     assert lib.gpp_set_dropin_precision(3) == capi.GPP_ERR_INVALID_ARGUMENT
     assert lib.gpp_set_dropin_precision(-1) == capi.GPP_OK

@@ -88,7 +88,8 @@ def test_full_production_shape_matches_reference(case):
 def test_full_production_shape_band_independent_gemm_paths():
     """The production shape with one wx row for every band (the reference's
     wx_array[3], so every drop-in entry point's case): the FP64 band-sum GEMM
-    path agrees with the per-term FP64 kernel within 1e-12, the mixed
+    path -- its GEMMs on the tensor cores (mode 1) and on the FP64 pipe
+    (mode 2) -- agrees with the per-term FP64 kernel within 1e-12, the mixed
     float-float GEMM path with FP64 within 1e-10, per component, and the
     per-band outputs likewise (norm-wise)."""
     from gppsigma import ops as o
@@ -99,7 +100,7 @@ def test_full_production_shape_band_independent_gemm_paths():
     res = {}
     try:
         for label, precision, mode in (("perterm", "fp64", 0), ("gemm", "fp64", 1),
-                                       ("mixed_gemm", "mixed", 1)):
+                                       ("gemm_fp64_pipe", "fp64", 2), ("mixed_gemm", "mixed", 1)):
             capi.check(lib.gpp_set_gemm_path(mode), "gpp_set_gemm_path")
             r = o.sigma(d, precision, acht_n1=True)
             o.wait()
@@ -107,7 +108,8 @@ def test_full_production_shape_band_independent_gemm_paths():
     finally:
         capi.check(lib.gpp_set_gemm_path(-1), "gpp_set_gemm_path")
     ref = res["perterm"]
-    for label, tol in (("gemm", FP64_TOL), ("mixed_gemm", MIXED_DELIVERED)):
+    for label, tol in (("gemm", FP64_TOL), ("gemm_fp64_pipe", FP64_TOL),
+                       ("mixed_gemm", MIXED_DELIVERED)):
         for k in ("achtemp", "asxtemp"):
             assert rel_err(res[label][k], ref[k]) <= tol, (label, k)
         assert norm_err(res[label]["acht_n1_loc"], ref["acht_n1_loc"]) <= tol, label

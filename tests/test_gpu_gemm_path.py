@@ -1,7 +1,9 @@
 """The band-sum GEMM path of FP64 calls with band-independent frequencies:
 the same sums as the per-term kernel and the oracle (achtemp, asxtemp,
 acht_n1_loc, the static term), on ragged shapes, clamped G' indices,
-near-pole wtilde, every frequency-chunk width and the overlapped host path."""
+near-pole wtilde, every frequency-chunk width and the overlapped host path;
+with the GEMMs on the tensor cores (the default, mode 1) and on the FP64
+pipe (mode 2)."""
 import dataclasses
 
 import numpy as np
@@ -59,17 +61,18 @@ def test_gemm_path_equals_per_term_kernel_and_oracle(shape, semantics):
     d = ops.DeviceInputs.from_host(inp)
     assert d.wx_stride == 0
     n1 = shape.nw >= 3
-    g = sigma_with(1, d, semantics, n1)
     t = sigma_with(0, d, semantics, n1)
-    for key in ("achtemp", "asxtemp", "achstemp"):
-        a, b = getattr(g, key).cpu().numpy(), getattr(t, key).cpu().numpy()
-        assert rel_err(a, want[key]) <= FP64_TOL, key
-        assert rel_err(a, b) <= FP64_TOL, key
-    if n1:
-        a = g.acht_n1_loc.cpu().numpy()
-        scale = np.max(np.abs(want["acht_n1_loc"]))
-        assert np.max(np.abs(a - want["acht_n1_loc"])) <= FP64_TOL * scale
-        assert np.max(np.abs(a - t.acht_n1_loc.cpu().numpy())) <= FP64_TOL * scale
+    for mode in (1, 2):
+        g = sigma_with(mode, d, semantics, n1)
+        for key in ("achtemp", "asxtemp", "achstemp"):
+            a, b = getattr(g, key).cpu().numpy(), getattr(t, key).cpu().numpy()
+            assert rel_err(a, want[key]) <= FP64_TOL, (mode, key)
+            assert rel_err(a, b) <= FP64_TOL, (mode, key)
+        if n1:
+            a = g.acht_n1_loc.cpu().numpy()
+            scale = np.max(np.abs(want["acht_n1_loc"]))
+            assert np.max(np.abs(a - want["acht_n1_loc"])) <= FP64_TOL * scale, mode
+            assert np.max(np.abs(a - t.acht_n1_loc.cpu().numpy())) <= FP64_TOL * scale, mode
 
 
 def test_gemm_path_is_bit_reproducible_and_automatic_from_32_bands():
@@ -82,7 +85,7 @@ def test_gemm_path_is_bit_reproducible_and_automatic_from_32_bands():
         x, y, z = (getattr(r, key).cpu().numpy() for r in (a, b, g))
         assert np.array_equal(x, y) and np.array_equal(x, z), key
     lib = capi.load()
-    assert lib.gpp_set_gemm_path(2) == capi.GPP_ERR_INVALID_ARGUMENT
+    assert lib.gpp_set_gemm_path(3) == capi.GPP_ERR_INVALID_ARGUMENT
 
 
 @pytest.mark.parametrize("ngpown", [33, 4])

@@ -1,0 +1,124 @@
+"""The integer slicing of the tensor-core FP64 GEMM (gpp_ozaki_split.cuh),
+compiled for the host from the same header the kernels use: for doubles of
+every magnitude, sign and subnormal, and chunk exponents e with |x| < 2^e,
+the slices reconstruct x = 2^e sum_i s_i 2^(-7 i) to within 2^(e - 57)
+(checked exactly, in 128-bit integers), s_1 lies in [-128, 128] and the others
+in [-64, 63] (the bounds the exact group sums rest on), and every slice is an
+integer that bf16 holds exactly.  The group table of gpp_ozaki.cu is checked
+against those bounds: each group's worst-case sum over 512 k values stays
+within 2^24, where FP32 accumulation is exact.
+"""
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import REPO
+
+CSRC = os.path.join(REPO, "doe-csfg-hackathon_gb300", "csrc")
+
+HARNESS = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include "gpp_ozaki_split.cuh"
+
+static unsigned long long st = 31;
+static unsigned long long nx() {
+    unsigned long long z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int main() {
+    int bad = 0;
+    const int n = 2000000;
+    for (int t = 0; t < n; ++t) {
+        double x;
+        unsigned long long u = nx();
+        switch (t % 4) {
+            case 0: x = ldexp((double)(u >> 11) / 9007199254740992.0, (int)(nx() % 80) - 40); break;
+            case 1: memcpy(&x, &u, 8); if (!std::isfinite(x)) x = 1.0; break;  // any finite double
+            case 2: x = ldexp(1.0, (int)(nx() % 2000) - 1000) * ((u & 1) ? 1 : -1); break;
+            default: x = ldexp((double)(u % 1000003), -1074 + (int)(nx() % 40)); break;  // subnormals
+        }
+        if (u & 2) x = -x;
+        int e = 0;
+        if (x != 0.0) frexp(x, &e);
+        e += (int)(nx() % 3);  // the chunk's exponent may exceed this value's
+        int d[gpp::kOzSlices];
+        gpp::oz_slices(x, e, d);
+        // sum_i d_i 2^(7 (S - i)) vs x 2^(7 S - e), exactly: x = m 2^ex.
+        __int128 sum = 0;
+        for (int i = 0; i < gpp::kOzSlices; ++i) {
+            const int lo = i == 0 ? -128 : -64, hi = i == 0 ? 128 : 63;
+            if (d[i] < lo || d[i] > hi) { if (bad++ < 5) printf("digit %d = %d out of range\n", i, d[i]); }
+            sum = sum * 128 + d[i];
+        }
+        int ex;
+        const double f = frexp(fabs(x), &ex);  // |x| = f 2^ex, f in [0.5, 1)
+        const long long m = (long long)ldexp(f, 53);  // |x| = m 2^(ex - 53)
+        const int sh = ex - 53 + 7 * gpp::kOzSlices - e;  // x 2^(7S - e) = m 2^sh
+        // |sum - sign m 2^sh| <= 1/2, compared as (2 sum - 2 sign m 2^sh) in units of 2^min(sh, 0)
+        __int128 lhs = 2 * sum, rhs = (__int128)(x < 0 ? -m : m) * 2;
+        if (sh >= 0) {
+            rhs <<= sh;
+            if (lhs != rhs) { if (bad++ < 5) printf("x %a e %d: not exact\n", x, e); }
+        } else if (sh > -100) {
+            lhs <<= -sh;
+            __int128 diff = lhs - rhs;
+            if (diff < 0) diff = -diff;
+            if (diff > ((__int128)1 << -sh)) { if (bad++ < 5) printf("x %a e %d: error above half a unit\n", x, e); }
+        } else if (sum != 0) {
+            if (bad++ < 5) printf("x %a e %d: tiny value gave slices\n", x, e);
+        }
+    }
+    printf("%d failures\n", bad);
+    return bad ? 1 : 0;
+}
+"""
+
+
+def test_slices_reconstruct_and_stay_in_range(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    src = tmp_path / "ozaki_split_check.cu"
+    src.write_text(HARNESS)
+    exe = tmp_path / "ozaki_split_check"
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-I", CSRC, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "0 failures" in out.stdout
+
+
+def _table(name, text):
+    m = re.search(name + r"\[kPairs\] = \{([^}]*)\}", text) or re.search(name + r"\[kGroups\] = \{([^}]*)\}", text)
+    return [int(v) for v in m.group(1).replace("\n", " ").split(",")]
+
+
+def test_group_table_sums_fit_in_fp32():
+    text = open(os.path.join(CSRC, "gpp_ozaki.cu")).read()
+    pi, pj, end = _table("kPairI", text), _table("kPairJ", text), _table("kGroupEnd", text)
+    gd = _table("kGroupD", text)
+    kc = int(re.search(r"constexpr int kKcMax = (\d+);", text).group(1))
+    bound = lambda i: 128 if i == 1 else 64
+    pairs = set(zip(pi, pj))
+    # every pair with i + j <= S + 1 exactly once, none beyond
+    assert len(pairs) == len(pi) == 36
+    assert pairs == {(i, j) for i in range(1, 9) for j in range(1, 9) if i + j <= 9}
+    groups, cur = [], []
+    for i, j, e in zip(pi, pj, end):
+        cur.append((i, j))
+        if e:
+            groups.append(cur)
+            cur = []
+    assert not cur and len(groups) == len(gd) == 10
+    for g, d in zip(groups, gd):
+        assert all(i + j == d for i, j in g)
+        assert sum(bound(i) * bound(j) for i, j in g) * kc <= 2 ** 24
