@@ -218,6 +218,16 @@ bool overlap_occupied() {
     return on;
 }
 
+// Whether FP64 calls whose band sum runs on the tensor cores run the FP64
+// occupied-band kernel concurrently on the side stream (the default), so
+// that the FP64 pipe and the tensor cores work at the same time;
+// GPP_OVERLAP_FP64_GEMM=0 runs it first on the caller's stream.  Read on
+// every call.
+bool overlap_fp64_gemm() {
+    const char *v = getenv("GPP_OVERLAP_FP64_GEMM");
+    return !(v && v[0] == '0');
+}
+
 gpp_status side_stream(int dev, SideStream **out) {
     if (t_side.dev != dev) {
         int lo = 0, hi = 0;
@@ -315,7 +325,10 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     if (e == cudaSuccess && mixed)  // float-float planes of every band the call touches
         e = launch_split_bands(p, w + o_split, has_flag ? fb0 : nb0, has_noflag ? nb1 : fb1, s);
     SideStream *side = nullptr;
-    const bool overlap = mixed && has_flag && has_noflag && overlap_occupied() && !pieces;
+    const bool overlap =
+        has_flag && has_noflag && !pieces &&
+        (mixed ? overlap_occupied()
+               : gemm && fp64_gemm_on_tensor_cores() && overlap_fp64_gemm());
     RowPieces whole;
     whole.n = 1;
     whole.pair[0] = 0;
@@ -377,7 +390,9 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     if (e == cudaSuccess && overlap) {
         e = cudaStreamWaitEvent(side->st, side->fork, 0);
         part.ach_tile0 = 0;
-        if (e == cudaSuccess) e = launch_flag_mixed(p, part, w + o_split, side->st);
+        if (e == cudaSuccess)
+            e = mixed ? launch_flag_mixed(p, part, w + o_split, side->st)
+                      : launch_flag_fp64(p, part, side->st);
         if (e == cudaSuccess) e = cudaEventRecord(side->join, side->st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, side->join, 0);
     }

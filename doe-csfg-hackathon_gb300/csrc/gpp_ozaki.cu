@@ -150,8 +150,9 @@ __device__ __forceinline__ int exp_of_bits(unsigned long long b) {
 // Largest |re|, |im|, |re + im| of Z(l, k) over chunk c, as an exponent e
 // with max < 2^e (kZeroExp when the chunk is all zero), for l < Lp (rows
 // past L are zero); compared as bit patterns on the integer pipes.  kfast: a
-// warp per (l, c), lanes along k; else a thread per (l, c), consecutive
-// threads on consecutive l.
+// warp per (l, c), lanes along k; else a block per (c, 32 consecutive l):
+// lanes along l, the 8 warps interleaved along k, reduced through shared
+// memory.
 __global__ void __launch_bounds__(256) oz_exp_kernel(OzOperand z, int K, int Kc, int nch, int Lp,
                                                      int *E) {
     const long long n = (long long)nch * Lp;
@@ -169,14 +170,23 @@ __global__ void __launch_bounds__(256) oz_exp_kernel(OzOperand z, int K, int Kc,
             if (lane == 0) E[w] = exp_of_bits(mx);
         }
     } else {
-        for (long long w = (long long)blockIdx.x * 256 + threadIdx.x; w < n;
-             w += (long long)gridDim.x * 256) {
-            const int c = (int)(w / Lp), l = (int)(w % Lp);
+        __shared__ unsigned long long red[8][32];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        const int tiles = Lp / 32;  // Lp is a multiple of the block tile
+        for (int b = blockIdx.x; b < nch * tiles; b += gridDim.x) {
+            const int c = b / tiles, l = (b % tiles) * 32 + lane;
             unsigned long long mx = 0;
             if (l < z.L)
-                for (int k = c * Kc; k < min(K, (c + 1) * Kc); ++k)
+                for (int k = c * Kc + warp; k < min(K, (c + 1) * Kc); k += 8)
                     mx = max(mx, max3_bits(operand_at(z, l, k)));
-            E[w] = exp_of_bits(mx);
+            red[warp][lane] = mx;
+            __syncthreads();
+            if (warp == 0) {
+#pragma unroll
+                for (int w = 1; w < 8; ++w) mx = max(mx, red[w][lane]);
+                E[(size_t)c * Lp + l] = exp_of_bits(mx);
+            }
+            __syncthreads();
         }
     }
 }
@@ -443,9 +453,10 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
     if (g.Mp / kBM > 65535 || g.Np / kBN > 65535 || g.splits > 65535)
         return cudaErrorInvalidConfiguration;
     const Buffers b = carve(g, ws);
-    oz_exp_kernel<<<grid_for((long long)g.nch * g.Mp * (X.kfast ? 32 : 1)), 256, 0, s>>>(
+    // kfast: a warp per (row, chunk); else a block per (chunk, 32 rows).
+    oz_exp_kernel<<<grid_for((long long)g.nch * g.Mp * (X.kfast ? 32 : 8)), 256, 0, s>>>(
         X, K, g.Kc, g.nch, g.Mp, b.ex);
-    oz_exp_kernel<<<grid_for((long long)g.nch * g.Np * (Y.kfast ? 32 : 1)), 256, 0, s>>>(
+    oz_exp_kernel<<<grid_for((long long)g.nch * g.Np * (Y.kfast ? 32 : 8)), 256, 0, s>>>(
         Y, K, g.Kc, g.nch, g.Np, b.ey);
     oz_emax_kernel<<<grid_for(g.Mp), 256, 0, s>>>(b.ex, g.nch, g.Mp, b.exmax);
     oz_emax_kernel<<<grid_for(g.Np), 256, 0, s>>>(b.ey, g.nch, g.Np, b.eymax);
