@@ -218,13 +218,13 @@ bool overlap_occupied() {
     return on;
 }
 
-// Whether FP64 calls whose band sum runs on the tensor cores run the FP64
+// Whether calls whose band sum runs on the tensor cores run the
 // occupied-band kernel concurrently on the side stream (the default), so
-// that the FP64 pipe and the tensor cores work at the same time;
-// GPP_OVERLAP_FP64_GEMM=0 runs it first on the caller's stream.  Read on
+// that the FP64 / FP32 pipes and the tensor cores work at the same time;
+// GPP_OVERLAP_TENSOR_GEMM=0 runs it first on the caller's stream.  Read on
 // every call.
-bool overlap_fp64_gemm() {
-    const char *v = getenv("GPP_OVERLAP_FP64_GEMM");
+bool overlap_tensor_gemm() {
+    const char *v = getenv("GPP_OVERLAP_TENSOR_GEMM");
     return !(v && v[0] == '0');
 }
 
@@ -298,9 +298,14 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const size_t o_n1 = off; off = align_up(off + (want_n1 ? sizeof(double2) * (size_t)(n1_seg * p.nb) : 0));
     const size_t o_st = off; off = align_up(off + sizeof(double2) * (size_t)achs_blocks);
     const size_t o_split = off; off = align_up(off + (mixed ? mixed_split_bytes(p) : 0));
-    const size_t gemm_ws = !gemm ? 0 : mixed ? mixed_gemm_bytes(p, nb1 - nb0, want_n1)
+    // Band sums on the tensor cores (both precisions; mixed precision then
+    // splits G into its float-float planes) unless gpp_set_gemm_path(2).
+    const bool tensor = gemm && fp64_gemm_on_tensor_cores();
+    const size_t gemm_ws = !gemm ? 0 : mixed ? mixed_gemm_bytes(p, nb1 - nb0, want_n1 && !tensor)
                                             : gemm_bytes(p, nb1 - nb0, want_n1);
     const size_t o_gemm = off; off = align_up(off + gemm_ws);
+    const size_t o_gemm64 = off;
+    off = align_up(off + (mixed && tensor ? gemm_bytes(p, nb1 - nb0, want_n1) : 0));
     const size_t ws_bytes = off > 0 ? off : 256;
 
     void *ws = nullptr;
@@ -327,8 +332,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     SideStream *side = nullptr;
     const bool overlap =
         has_flag && has_noflag && !pieces &&
-        (mixed ? overlap_occupied()
-               : gemm && fp64_gemm_on_tensor_cores() && overlap_fp64_gemm());
+        (gemm && tensor ? overlap_tensor_gemm() : mixed && overlap_occupied());
     RowPieces whole;
     whole.n = 1;
     whole.pair[0] = 0;
@@ -359,11 +363,20 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
             if (k == 0 && t_timing && t_ev0) cudaEventRecord(t_ev0, s);
             if (gemm && mixed) {
                 st = GPP_OK;
-                if (k == 0) st = mixed_gemm_band_sum(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
+                if (k == 0 && tensor) {
+                    st = gemm_band_sum(p, part, w + o_gemm64, nb0, nb1, s);
+                    if (st == GPP_OK)
+                        st = mixed_gemm_planes_from(
+                            p, w + o_gemm, nb0, nb1,
+                            gemm_g(p, w + o_gemm64, nb1 - nb0, want_n1), s);
+                } else if (k == 0) {
+                    st = mixed_gemm_band_sum(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
+                }
                 if (st == GPP_OK)
                     st = mixed_gemm_rows(p, part, w + o_split, w + o_gemm, nb0, nb1, s, rt);
                 if (st == GPP_OK && k == pc.n - 1)
-                    st = mixed_gemm_per_band(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
+                    st = tensor ? gemm_per_band(p, part, w + o_gemm64, nb0, nb1, s)
+                                : mixed_gemm_per_band(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
                 if (st != GPP_OK) {
                     cudaFreeAsync(ws, s);
                     return st;

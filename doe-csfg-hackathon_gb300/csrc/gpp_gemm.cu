@@ -380,6 +380,10 @@ GemmBuffers carve(const Problem &p, void *ws, int K, bool want_n1) {
 
 }  // namespace
 
+const double2 *gemm_g(const Problem &p, void *ws, int bands, bool want_n1) {
+    return carve(p, ws, bands, want_n1).G;
+}
+
 gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
                          cudaStream_t s) {
     const int K = b1 - b0;

@@ -33,4 +33,8 @@ gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, i
 gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b0, int b1,
                          cudaStream_t s);
 
+// G (ng x nc, FP64) inside a workspace of gemm_bytes(p, bands, want_n1),
+// written by gemm_band_sum.
+const double2 *gemm_g(const Problem &p, void *ws, int bands, bool want_n1);
+
 }  // namespace gpp

@@ -271,6 +271,24 @@ __global__ void __launch_bounds__(128) mg_freq_kernel(Problem p, Partials part, 
             make_double2(S[w * 2], S[w * 2 + 1]);
 }
 
+// G's row-pair planes (re, im; lanes the pair's rows, hi then lo) from an
+// FP64 G [ng][nc]; a row past ngpown is 0.
+__global__ void __launch_bounds__(kThreads) mg_planes_kernel(const double2 *G, int ng, int nc,
+                                                             float4 *Gp) {
+    const int pairs = (ng + 1) / 2;
+    const size_t n = (size_t)pairs * nc;
+    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * kThreads) {
+        const size_t j = i / nc, col = i % nc;
+        const double2 g0 = G[2 * j * nc + col];
+        const double2 g1 = 2 * j + 1 < (size_t)ng ? G[(2 * j + 1) * nc + col] : make_double2(0.0, 0.0);
+        const df a0 = split_bits(g0.x), a1 = split_bits(g1.x);
+        const df b0 = split_bits(g0.y), b1 = split_bits(g1.y);
+        Gp[j * 2 * nc + col] = make_float4(a0.h, a1.h, a0.l, a1.l);
+        Gp[j * 2 * nc + nc + col] = make_float4(b0.h, b1.h, b0.l, b1.l);
+    }
+}
+
 // M_2[j][ig] = Q conj(wdiff) / |wdiff|^2 at iw = 2 for row pair j, in
 // float-float lanes (FP64 from the inputs within 1e-3 |wx| of the pole),
 // stored as two planes (re, im) per row pair.
@@ -456,6 +474,17 @@ gpp_status mixed_gemm_band_sum(const Problem &p, const Partials &part, void *spl
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "mg_gemm_kernel");
     return GPP_OK;
+}
+
+gpp_status mixed_gemm_planes_from(const Problem &p, void *ws, int b0, int b1, const double2 *G,
+                                  cudaStream_t st) {
+    const int K = b1 - b0, pairs = row_pairs(p);
+    if (K <= 0 || pairs <= 0) return GPP_OK;
+    mg_planes_kernel<<<grid_for((long long)pairs * p.nc), kThreads, 0, st>>>(G, p.ng, p.nc,
+                                                                          planes_g(p, ws, K));
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GPP_OK : cuda_fail(e, "mg_planes_kernel");
 }
 
 gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_ws, void *ws, int b0,

@@ -31,4 +31,10 @@ gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_w
 gpp_status mixed_gemm_per_band(const Problem &p, const Partials &part, void *split_ws, void *ws,
                                int b0, int b1, cudaStream_t st);
 
+// Step 1 from an FP64 G (ng x nc) computed elsewhere (the tensor-core band
+// sum of gpp_gemm.cu): G split into the float-float row-pair planes that
+// mixed_gemm_rows reads, in `ws` of mixed_gemm_bytes(p, b1 - b0, false).
+gpp_status mixed_gemm_planes_from(const Problem &p, void *ws, int b0, int b1, const double2 *G,
+                                  cudaStream_t st);
+
 }  // namespace gpp

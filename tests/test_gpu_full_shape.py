@@ -90,8 +90,9 @@ def test_full_production_shape_band_independent_gemm_paths():
     wx_array[3], so every drop-in entry point's case): the FP64 band-sum GEMM
     path -- its GEMMs on the tensor cores (mode 1) and on the FP64 pipe
     (mode 2) -- agrees with the per-term FP64 kernel within 1e-12, the mixed
-    float-float GEMM path with FP64 within 1e-10, per component, and the
-    per-band outputs likewise (norm-wise)."""
+    paths (tensor-core G split to float-float; the float-float GEMM) with FP64
+    within 1e-10, per component, and the per-band outputs likewise
+    (norm-wise)."""
     from gppsigma import ops as o
     lib = capi.load()
     d = o.device_inputs(W.CONFIGS["production"], 20240607)
@@ -100,7 +101,8 @@ def test_full_production_shape_band_independent_gemm_paths():
     res = {}
     try:
         for label, precision, mode in (("perterm", "fp64", 0), ("gemm", "fp64", 1),
-                                       ("gemm_fp64_pipe", "fp64", 2), ("mixed_gemm", "mixed", 1)):
+                                       ("gemm_fp64_pipe", "fp64", 2), ("mixed_gemm", "mixed", 1),
+                                       ("mixed_gemm_fp32", "mixed", 2)):
             capi.check(lib.gpp_set_gemm_path(mode), "gpp_set_gemm_path")
             r = o.sigma(d, precision, acht_n1=True)
             o.wait()
@@ -109,7 +111,7 @@ def test_full_production_shape_band_independent_gemm_paths():
         capi.check(lib.gpp_set_gemm_path(-1), "gpp_set_gemm_path")
     ref = res["perterm"]
     for label, tol in (("gemm", FP64_TOL), ("gemm_fp64_pipe", FP64_TOL),
-                       ("mixed_gemm", MIXED_DELIVERED)):
+                       ("mixed_gemm", MIXED_DELIVERED), ("mixed_gemm_fp32", MIXED_DELIVERED)):
         for k in ("achtemp", "asxtemp"):
             assert rel_err(res[label][k], ref[k]) <= tol, (label, k)
         assert norm_err(res[label]["acht_n1_loc"], ref["acht_n1_loc"]) <= tol, label

@@ -136,20 +136,23 @@ def mixed_with(mode, d, semantics, n1=False):
     (W.Shape(300, 0, 4099, 5, 4, near_pole=0.05), "complex_seq"),
 ])
 def test_mixed_gemm_path_within_1e8_of_fp64(shape, semantics):
-    """The float-float band-sum GEMM against the FP64 per-term kernel."""
+    """The mixed-precision band-sum paths -- G from the tensor cores split
+    into float-float (mode 1) and the float-float GEMM (mode 2) -- against
+    the FP64 per-term kernel and the mixed per-term kernel."""
     from gppsigma import ops
     d = ops.DeviceInputs.from_host(band_independent(shape, 93))
     n1 = shape.nw >= 3
-    m = mixed_with(1, d, semantics, n1)
     f = sigma_with(0, d, semantics, n1)
     t = mixed_with(0, d, semantics, n1)
-    for key in ("achtemp", "asxtemp"):
-        a = getattr(m, key).cpu().numpy()
-        assert rel_err(a, getattr(f, key).cpu().numpy()) <= MIXED_TOL, key
-        assert rel_err(a, getattr(t, key).cpu().numpy()) <= MIXED_TOL, key
-    if n1:  # per-band output (norm-wise: single bands cancel more than the sums)
-        a, w = m.acht_n1_loc.cpu().numpy(), f.acht_n1_loc.cpu().numpy()
-        assert np.max(np.abs(a - w)) <= MIXED_TOL * np.max(np.abs(w))
+    for mode in (1, 2):
+        m = mixed_with(mode, d, semantics, n1)
+        for key in ("achtemp", "asxtemp"):
+            a = getattr(m, key).cpu().numpy()
+            assert rel_err(a, getattr(f, key).cpu().numpy()) <= MIXED_TOL, (mode, key)
+            assert rel_err(a, getattr(t, key).cpu().numpy()) <= MIXED_TOL, (mode, key)
+        if n1:  # per-band output (norm-wise: single bands cancel more than the sums)
+            a, w = m.acht_n1_loc.cpu().numpy(), f.acht_n1_loc.cpu().numpy()
+            assert np.max(np.abs(a - w)) <= MIXED_TOL * np.max(np.abs(w)), mode
 
 
 def test_mixed_gemm_path_through_the_host_pieces():
