@@ -397,7 +397,7 @@ gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b
     // G (ng x nc) = C^T aqsn: X(r, k) = C[k][r], Y(ig, k) = aqsn[b0 + k][ig].
     if (fp64_gemm_on_tensor_cores()) {
         const OzOperand X{b.C, p.ng, false, p.ng}, Y{p.aqsn + (size_t)b0 * p.nc, p.nc, false, p.nc};
-        e = ozaki_zgemm(X, Y, p.ng, p.nc, K, 1, b.G, p.nc, 0, b.oz, s);
+        e = ozaki_zgemm(X, Y, p.ng, p.nc, K, 1, b.G, p.nc, 0, b.oz, part.err, s);
         if (e != cudaSuccess) return cuda_fail(e, "ozaki_zgemm (band sum)");
         return GPP_OK;
     }
@@ -439,7 +439,7 @@ gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b
     if (fp64_gemm_on_tensor_cores()) {
         const OzOperand X{p.aqsn + (size_t)b0 * p.nc, p.nc, true, K}, Y{b.M2, p.nc, true, p.ng};
         e = ozaki_zgemm(X, Y, K, p.ng, p.nc, kHSplitsTensor, b.H, p.ng, (long long)K * p.ng, b.oz,
-                        s);
+                        part.err, s);
         if (e != cudaSuccess) return cuda_fail(e, "ozaki_zgemm (per-band output)");
         splits = ozaki_splits(p.nc, kHSplitsTensor);
     } else {

@@ -16,7 +16,7 @@
 //  * a product of two slices summed over a chunk of at most 512 k values is
 //    an integer below 2^24 in magnitude, which the tensor cores' FP32
 //    accumulation adds exactly (checked on the GB300 for sums up to 2^24
-//    with operands up to 128);
+//    with operands up to 128, with mma.sync and with tcgen05.mma);
 //  * pairs (i, j) with the same i + j = d share the scale 2^(-7 d); those
 //    whose worst-case sums still fit in 2^24 are summed in one accumulator
 //    (10 groups for the 36 pairs with i + j <= 9), each group's exact
@@ -28,13 +28,15 @@
 // Complex products take the 3M form (Gauss: re = P1 - P2, im = P3 - P1 -
 // P2 with P1 = sum xr yr, P2 = sum xi yi, P3 = sum (xr + xi)(yr + yi)), so
 // three real splittings and three real products, as in zgemm3m_kernel; the
-// result agrees with that FP64 GEMM to about 1e-15 of its values.
+// result agrees with that FP64 GEMM to about 1e-14 of its values.
 //
-// The tensor-core kernel uses warp-level mma.sync m16n8k16 (bf16 in, FP32
-// accumulate): a block of 4 warps computes 128 x 128 outputs (64 x 64 per
-// warp), staging 32 k of one slice pair per step through a four-stage
-// cp.async ring in shared memory (rows padded to 80 bytes so ldmatrix is
-// conflict-free), two blocks per SM.
+// The tensor-core kernel is tcgen05-native: tcgen05.mma kind::f16 (bf16 in,
+// FP32 accumulate in tensor memory), M = 128 x N = 256 per instruction,
+// issued by one thread; operands staged by 1-D bulk copies (the slicing pass
+// writes each pipeline stage's operand block contiguously, already in the
+// no-swizzle core-matrix layout the MMA descriptors describe) through a
+// four-stage mbarrier ring; two TMEM accumulators so four epilogue warps
+// drain one group (tcgen05.ld) while the next is being summed.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -51,12 +53,15 @@ namespace {
 
 constexpr int kS = kOzSlices;    // slices per operand value
 constexpr int kKcMax = 512;      // k values per chunk (exactness bound)
-constexpr int kBM = 128, kBN = 128, kBK = 32;
-constexpr int kThreads = 128;    // 4 warps: 2 along M x 2 along N, 64 x 64 each
-constexpr int kLdk = kBK + 8;    // padded shared-memory row (80 bytes)
-constexpr int kStages = 4;
-constexpr size_t kGemmSmem = sizeof(__nv_bfloat16) * kStages * (kBM + kBN) * kLdk;  // 80 KB
 constexpr int kGroups = 10;      // fold groups per (plane, chunk)
+
+// The tensor-core tile: tcgen05.mma M = 128 (rows of X), N = 256 (rows of
+// Y), 64 k per pipeline stage (four K = 16 instructions), four stages.
+constexpr int kTM = 128, kTN = 256, kTK = 64, kTStages = 4;
+constexpr unsigned kStageA = kTM * kTK * 2, kStageB = kTN * kTK * 2;  // 16 KB, 32 KB
+constexpr size_t kTcSmem = (size_t)kTStages * (kStageA + kStageB) + 256;
+constexpr int kTcThreads = 192;  // warp 0 loads, warp 1 issues the MMAs, warps 2-5 drain TMEM
+constexpr int kTmemCols = 2 * kTN;  // two accumulators of 256 FP32 columns
 
 // The 36 slice pairs (i, j), i + j <= 9, in group order; kGroupEnd marks the
 // last pair of each group (the fold point, scale 2^(-7 (i + j))).  Group
@@ -75,7 +80,7 @@ __constant__ unsigned char kGroupD[kGroups] = {2, 3, 4, 5, 6, 7, 8, 8, 9, 9};
 struct Geometry {
     int M, N, K;       // logical sizes
     int Mp, Np;        // padded to the block tile
-    int nch, Kc, Kp;   // chunks, chunk length (multiple of kBK), padded K = nch * Kc
+    int nch, Kc, Kp;   // chunks, chunk length (multiple of kTK), padded K = nch * Kc
     int cps, splits;   // chunks per split, splits
 };
 
@@ -84,10 +89,10 @@ Geometry geometry(int M, int N, int K, int splits) {
     g.M = M;
     g.N = N;
     g.K = K;
-    g.Mp = ceil_div(std::max(M, 1), kBM) * kBM;
-    g.Np = ceil_div(std::max(N, 1), kBN) * kBN;
+    g.Mp = ceil_div(std::max(M, 1), kTM) * kTM;
+    g.Np = ceil_div(std::max(N, 1), kTN) * kTN;
     g.nch = std::max(1, ceil_div(K, kKcMax));
-    g.Kc = ceil_div(ceil_div(std::max(K, 1), g.nch), kBK) * kBK;
+    g.Kc = ceil_div(ceil_div(std::max(K, 1), g.nch), kTK) * kTK;
     g.Kp = g.nch * g.Kc;
     g.cps = ceil_div(g.nch, std::max(1, splits));
     g.splits = ceil_div(g.nch, g.cps);
@@ -200,19 +205,33 @@ __global__ void __launch_bounds__(256) oz_emax_kernel(const int *E, int nch, int
     }
 }
 
-// Slices of the three real planes (re, im, re + im): out[((g S + i) Lp + l)
-// Kp + k] = s_(i+1) of plane g at (l, k); zero outside L x K.  The slices
-// are the balanced base-128 digits of round(x 2^(7 S - e)): s_2..s_S in
-// [-64, 63], s_1 the rest (|s_1| <= 128), so x = 2^e sum_i s_i 2^(-7 i) to
-// within 2^(e - 57).  Integer arithmetic throughout (the FP64 pipe is slow on
-// GB300).  A thread per (l, k), k fastest.
+// Position of (row l, k) in a slice plane, laid out for the tensor cores:
+// blocks of R rows x kTK k (R = kTM for X, kTN for Y), one block per
+// pipeline stage and so one bulk copy, ordered (row tile, k step); inside a
+// block the no-swizzle K-major core-matrix layout of tcgen05.mma -- core
+// matrices of 8 rows x 16 bytes, stored whole (128 bytes), the 8 k-cores of
+// a row group next to each other (1024 bytes per row group).
+__device__ __forceinline__ size_t tile_offset(int l, int k, int R, int Kp) {
+    const int rt = l / R, r = l % R, ks = k / kTK, kk = k % kTK;
+    return ((size_t)rt * (Kp / kTK) + ks) * ((size_t)R * kTK) +
+           (size_t)(((r >> 3) * (kTK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7));
+}
+
+// Slices of the three real planes (re, im, re + im): plane (g, i) holds
+// s_(i+1) of plane g at (l, k), at tile_offset(l, k) within it; zero outside
+// L x K.  The slices are the balanced base-128 digits of
+// round(x 2^(7 S - e)): s_2..s_S in [-64, 63], s_1 the rest (|s_1| <= 128),
+// so x = 2^e sum_i s_i 2^(-7 i) to within 2^(e - 57).  Integer arithmetic
+// throughout (the FP64 pipe is slow on GB300).  A thread per (l, k), k
+// fastest.
 __global__ void __launch_bounds__(256) oz_split_kernel(OzOperand z, int K, int Kc, int Kp, int Lp,
-                                                       const int *E, __nv_bfloat16 *out) {
+                                                       int R, const int *E, __nv_bfloat16 *out) {
     const long long n = (long long)Lp * Kp;
     const size_t plane = (size_t)Lp * Kp;
     for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
          t += (long long)gridDim.x * 256) {
         const int l = (int)(t / Kp), k = (int)(t % Kp);
+        const size_t at = tile_offset(l, k, R, Kp);
         double2 v = make_double2(0.0, 0.0);
         if (l < z.L && k < K) v = operand_at(z, l, k);
         const int e = E[(size_t)(k / Kc) * Lp + l];
@@ -223,37 +242,9 @@ __global__ void __launch_bounds__(256) oz_split_kernel(OzOperand z, int K, int K
             oz_slices(r[g], e, d);
 #pragma unroll
             for (int i = 0; i < kS; ++i)
-                out[(size_t)(g * kS + i) * plane + t] = __int2bfloat16_rn(d[i]);
+                out[(size_t)(g * kS + i) * plane + at] = __int2bfloat16_rn(d[i]);
         }
     }
-}
-
-__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
-    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
-__device__ __forceinline__ void ldmatrix_x4(unsigned (&r)[4], const void *p) {
-    const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0,
-                                         unsigned b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-        "{%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // 2^e as a float for e >= -126 (exact), 0 below (a group that far below the
@@ -271,115 +262,276 @@ __device__ __forceinline__ void df_acc(float &h, float &l, float v) {
     h = s;
 }
 
-// Position in a block's sequence of 32-k steps: plane g, chunk cl of the
-// split, slice pair p, k step ks (fastest).
-struct Step {
-    int ks, p, cl, g;
-    __device__ __forceinline__ void next(int KS, int nch_here) {
-        if (++ks < KS) return;
-        ks = 0;
-        if (++p < kPairs) return;
-        p = 0;
-        if (++cl < nch_here) return;
-        cl = 0;
-        ++g;
+// ---------------------------------------------------------------------------
+// tcgen05 / mbarrier primitives.
+__device__ __forceinline__ unsigned smem_addr(const void *p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void bar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void bar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void bar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool bar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for phase `parity`: gives up after kWaitLimit polls, or as soon
+// as another thread of the block raised *abort (and then raises it itself).
+__device__ __forceinline__ bool bar_wait(unsigned long long *bar, unsigned parity,
+                                         volatile int *abort) {
+    for (int it = 0; it < kWaitLimit; ++it) {
+        if (bar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63 && *abort) return false;
     }
+    *abort = 1;
+    return false;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Shared-memory matrix descriptor of tcgen05.mma for the no-swizzle K-major
+// layout: start address, LBO (bytes to the next core matrix along K), SBO
+// (bytes to the next 8-row group), the sm_100 descriptor version (bit 46).
+__device__ __forceinline__ unsigned long long umma_desc(unsigned saddr, unsigned lbo,
+                                                        unsigned sbo) {
+    return (unsigned long long)((saddr & 0x3FFFF) >> 4) |
+           ((unsigned long long)((lbo >> 4) & 0x3FFF) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+// Instruction descriptor of tcgen05.mma kind::f16: D FP32 (bits 4-5 = 1), A and
+// B bf16 (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr unsigned kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(kTN >> 3) << 17) |
+                            ((unsigned)(kTM >> 4) << 24);
+__device__ __forceinline__ void umma_bf16(unsigned tmem, unsigned long long a, unsigned long long b,
+                                          unsigned accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(unsigned long long *bar) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// Step t of a block's sequence (plane g, chunk cl of the split, slice pair p,
+// k step ks fastest).
+struct TcStep {
+    int g, cl, p, ks;
 };
+__device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
+    TcStep q;
+    q.ks = t % KS;
+    int r = t / KS;
+    q.p = r % kPairs;
+    r /= kPairs;
+    q.cl = r % nch_here;
+    q.g = r / nch_here;
+    return q;
+}
 
-// The tensor-core products: block (bx, by) of split z runs, for each real
-// plane g, chunk and slice pair, the 128 x 128 x 32 steps of the pair's
-// product, and stores each group's exact FP32 sum at
-// fold[((((z 3 + g) cps + cl) kGroups + group) Mp + m) Np + n].
-__global__ void __launch_bounds__(kThreads, 2)
-oz_gemm_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restrict__ SY,
-               int Mp, int Np, int Kp, int Kc, int cps, int nch, float *__restrict__ fold) {
-    extern __shared__ __align__(128) __nv_bfloat16 smem[];
-    __nv_bfloat16 (*sA)[kBM][kLdk] = reinterpret_cast<__nv_bfloat16 (*)[kBM][kLdk]>(smem);
-    __nv_bfloat16 (*sB)[kBN][kLdk] =
-        reinterpret_cast<__nv_bfloat16 (*)[kBN][kLdk]>(smem + (size_t)kStages * kBM * kLdk);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp >> 1, wn = warp & 1;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN, z = blockIdx.z;
+// The tensor-core products on tcgen05: block (bx, by, z) computes rows
+// [128 bx, +128) of X against rows [256 by, +256) of Y over split z's
+// chunks.  Warp 0 (one thread) streams each step's two operand blocks into a
+// four-stage shared-memory ring with 1-D bulk copies completing on full[s];
+// warp 1 (one thread) issues four K = 16 tcgen05.mma per step into one of two
+// TMEM accumulators (128 lanes x 256 FP32 columns each) and commits to
+// empty[s], and at a group's end to accfull[a]; warps 2-5 read a finished
+// accumulator (each warp its 32 TMEM lanes, 32 columns per tcgen05.ld),
+// store the group's exact sums at fold[((((z 3 + g) cps + cl) kGroups +
+// group) Mp + m) Np + n] and release it on accempty[a].  Every wait is
+// bounded; a block that gives up records kErrPipelineTimeout, lets its
+// copies and MMAs finish and frees its TMEM.
+__global__ void __launch_bounds__(kTcThreads, 1)
+oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restrict__ SY, int Mp,
+             int Np, int Kp, int Kc, int cps, int nch, float *__restrict__ fold, int *err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *sA = smem;
+    unsigned char *sB = smem + (size_t)kTStages * kStageA;
+    unsigned long long *bars =
+        reinterpret_cast<unsigned long long *>(smem + (size_t)kTStages * (kStageA + kStageB));
+    unsigned long long *full = bars, *empty = bars + kTStages;
+    unsigned long long *accfull = bars + 2 * kTStages, *accempty = accfull + 2;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(accempty + 2);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+    int *issued = abort_flag + 1, *consumed = abort_flag + 2;
+    volatile int *abort = abort_flag;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
     const int c0 = z * cps, nch_here = min(cps, nch - c0);
-    const int KS = Kc / kBK;
-    const long long T = 3LL * nch_here * kPairs * KS;
-    const size_t xplane = (size_t)Mp * Kp, yplane = (size_t)Np * Kp, fplane = (size_t)Mp * Np;
+    const int KS = Kc / kTK, ksteps = Kp / kTK;
+    const int T = 3 * nch_here * kPairs * KS;
+    const int NG = 3 * nch_here * kGroups;
 
-    Step ahead{0, 0, 0, 0};  // the next step to stage
-    auto issue = [&](int buf) {
-        const Step &q = ahead;
-        const size_t kof = (size_t)(c0 + q.cl) * Kc + (size_t)q.ks * kBK;
-        const __nv_bfloat16 *a =
-            SX + (size_t)(q.g * kS + kPairI[q.p] - 1) * xplane + (size_t)m0 * Kp + kof;
-        const __nv_bfloat16 *b =
-            SY + (size_t)(q.g * kS + kPairJ[q.p] - 1) * yplane + (size_t)n0 * Kp + kof;
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {  // 1024 16-byte pieces, 4 per 32-k row
-            const int piece = tid + r * kThreads;
-            const int row = (piece >> 2) & (kBM - 1), part16 = piece & 3;
-            if (piece < kBM * 4)
-                cp_async16(&sA[buf][row][part16 * 8], a + (size_t)row * Kp + part16 * 8);
-            else
-                cp_async16(&sB[buf][row][part16 * 8], b + (size_t)row * Kp + part16 * 8);
+    if (tid == 0) {
+        for (int s = 0; s < kTStages; ++s) {
+            bar_init(&full[s], 1);
+            bar_init(&empty[s], 1);
         }
-        ahead.next(KS, nch_here);
-    };
-
-    float acc[4][8][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.f;
-
-#pragma unroll
-    for (int st = 0; st < kStages - 1; ++st) {
-        if (st < T) issue(st);
-        cp_async_commit();
+        for (int a = 0; a < 2; ++a) {
+            bar_init(&accfull[a], 1);
+            bar_init(&accempty[a], 128);
+        }
+        *abort_flag = 0;
+        *issued = 0;
+        *consumed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    Step cur{0, 0, 0, 0};
-    int group = 0;
-    for (long long t = 0; t < T; ++t) {
-        cp_async_wait<kStages - 2>();
-        __syncthreads();  // step t has landed; every warp is done with step t - 1
-        if (t + kStages - 1 < T) issue((int)((t + kStages - 1) % kStages));
-        cp_async_commit();
-        const int buf = (int)(t % kStages);
-#pragma unroll
-        for (int kk = 0; kk < kBK; kk += 16) {
-            unsigned af[4][4], bfr[4][4];
-#pragma unroll
-            for (int mt = 0; mt < 4; ++mt)
-                ldmatrix_x4(af[mt], &sA[buf][wm * 64 + mt * 16 + (lane & 15)][kk + (lane >> 4) * 8]);
-#pragma unroll
-            for (int np = 0; np < 4; ++np)
-                ldmatrix_x4(bfr[np], &sB[buf][wn * 64 + np * 16 + (lane & 7) + ((lane >> 4) << 3)]
-                                        [kk + ((lane >> 3) & 1) * 8]);
-#pragma unroll
-            for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-                for (int nt = 0; nt < 8; ++nt)
-                    mma_bf16(acc[mt][nt], af[mt], bfr[nt >> 1][(nt & 1) * 2],
-                             bfr[nt >> 1][(nt & 1) * 2 + 1]);
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_addr(tmem_slot)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // producer
+            const size_t xplane = (size_t)Mp * Kp, yplane = (size_t)Np * Kp;
+            int t = 0;
+            for (; t < T; ++t) {
+                const int s = t % kTStages;
+                if (t >= kTStages && !bar_wait(&empty[s], ((t / kTStages) - 1) & 1, abort)) break;
+                const TcStep q = tc_decode(t, KS, nch_here);
+                const int ksg = (c0 + q.cl) * KS + q.ks;
+                const __nv_bfloat16 *a = SX + (size_t)(q.g * kS + kPairI[q.p] - 1) * xplane +
+                                         ((size_t)mt * ksteps + ksg) * (kTM * kTK);
+                const __nv_bfloat16 *b = SY + (size_t)(q.g * kS + kPairJ[q.p] - 1) * yplane +
+                                         ((size_t)nt * ksteps + ksg) * (kTN * kTK);
+                bar_expect_tx(&full[s], kStageA + kStageB);
+                bulk_g2s(sA + (size_t)s * kStageA, a, kStageA, &full[s]);
+                bulk_g2s(sB + (size_t)s * kStageB, b, kStageB, &full[s]);
+            }
+            *issued = t;
         }
-        if (cur.ks == KS - 1 && kGroupEnd[cur.p]) {  // store the group's exact sums
-            float *f = fold + ((((size_t)z * 3 + cur.g) * cps + cur.cl) * kGroups + group) * fplane;
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            int G = 0, t = 0;
+            for (; t < T; ++t) {
+                const int s = t % kTStages;
+                const TcStep q = tc_decode(t, KS, nch_here);
+                const bool first = q.ks == 0 && (q.p == 0 || kGroupEnd[q.p - 1]);
+                const bool last = q.ks == KS - 1 && kGroupEnd[q.p];
+                const int a = G & 1;
+                if (first && G >= 2 && !bar_wait(&accempty[a], ((G >> 1) - 1) & 1, abort)) break;
+                if (!bar_wait(&full[s], (t / kTStages) & 1, abort)) break;
+                tc_fence_after();
+                const unsigned sa = smem_addr(sA + (size_t)s * kStageA);
+                const unsigned sb = smem_addr(sB + (size_t)s * kStageB);
 #pragma unroll
-            for (int mt = 0; mt < 4; ++mt)
-#pragma unroll
-                for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int m = m0 + wm * 64 + mt * 16 + (lane >> 2) + h * 8;
-                        const int n = n0 + wn * 64 + nt * 8 + (lane & 3) * 2;
-                        *reinterpret_cast<float2 *>(f + (size_t)m * Np + n) =
-                            make_float2(acc[mt][nt][h * 2], acc[mt][nt][h * 2 + 1]);
-                        acc[mt][nt][h * 2] = acc[mt][nt][h * 2 + 1] = 0.f;
-                    }
-            group = group + 1 == kGroups ? 0 : group + 1;
+                for (int k16 = 0; k16 < kTK / 16; ++k16)
+                    umma_bf16(tmem + a * kTN, umma_desc(sa + k16 * 256, 128, 1024),
+                              umma_desc(sb + k16 * 256, 128, 1024), !(first && k16 == 0));
+                umma_commit(&empty[s]);
+                if (last) {
+                    umma_commit(&accfull[a]);
+                    ++G;
+                }
+            }
+            *consumed = t;
         }
-        cur.next(KS, nch_here);
+    } else {  // epilogue: warps 2-5, TMEM lanes 32 (warp % 4) ..
+        const int quarter = warp & 3;
+        const int m = mt * kTM + quarter * 32 + lane;
+        const size_t fplane = (size_t)Mp * Np;
+        for (int G = 0; G < NG; ++G) {
+            const int a = G & 1;
+            if (!bar_wait(&accfull[a], (G >> 1) & 1, abort)) break;
+            tc_fence_after();
+            const int grp = G % kGroups, q = G / kGroups;
+            const int cl = q % nch_here, g = q / nch_here;
+            float *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kGroups + grp) * fplane +
+                       (size_t)m * Np + (size_t)nt * kTN;
+            const unsigned ta = tmem + ((unsigned)(quarter * 32) << 16) + a * kTN;
+#pragma unroll 1
+            for (int c = 0; c < kTN; c += 32) {
+                float v[32];
+                tmem_ld32(ta + c, v);
+#pragma unroll
+                for (int j = 0; j < 32; j += 4)
+                    *reinterpret_cast<float4 *>(f + c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+            }
+            tc_fence_before();
+            bar_arrive(&accempty[a]);
+        }
+    }
+
+    __syncthreads();
+    if (*abort && tid == 0) {
+        atomicOr(err, kErrPipelineTimeout);
+        // Let the copies still in flight land and the issued MMAs finish.
+        for (int t = *consumed; t < *issued; ++t) {
+            int spin = 0;
+            while (!bar_try_wait(&full[t % kTStages], (unsigned)((t / kTStages) & 1)) &&
+                   ++spin < kWaitLimit) {
+            }
+        }
+        if (*consumed > 0) {
+            const int t = *consumed - 1;
+            int spin = 0;
+            while (!bar_try_wait(&empty[t % kTStages], (unsigned)((t / kTStages) & 1)) &&
+                   ++spin < kWaitLimit) {
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
     }
 }
 
@@ -446,11 +598,11 @@ size_t ozaki_bytes(int M, int N, int K, int splits) {
 int ozaki_splits(int K, int splits) { return geometry(1, 1, K, splits).splits; }
 
 cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, int K, int splits,
-                        double2 *Out, long long out_ld, long long split_stride, void *ws,
+                        double2 *Out, long long out_ld, long long split_stride, void *ws, int *err,
                         cudaStream_t s) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     const Geometry g = geometry(M, N, K, splits);
-    if (g.Mp / kBM > 65535 || g.Np / kBN > 65535 || g.splits > 65535)
+    if (g.Mp / kTM > 65535 || g.Np / kTN > 65535 || g.splits > 65535)
         return cudaErrorInvalidConfiguration;
     const Buffers b = carve(g, ws);
     // kfast: a warp per (row, chunk); else a block per (chunk, 32 rows).
@@ -460,23 +612,23 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
         Y, K, g.Kc, g.nch, g.Np, b.ey);
     oz_emax_kernel<<<grid_for(g.Mp), 256, 0, s>>>(b.ex, g.nch, g.Mp, b.exmax);
     oz_emax_kernel<<<grid_for(g.Np), 256, 0, s>>>(b.ey, g.nch, g.Np, b.eymax);
-    oz_split_kernel<<<grid_for((long long)g.Mp * g.Kp), 256, 0, s>>>(X, K, g.Kc, g.Kp, g.Mp, b.ex,
-                                                                    b.sx);
-    oz_split_kernel<<<grid_for((long long)g.Np * g.Kp), 256, 0, s>>>(Y, K, g.Kc, g.Kp, g.Np, b.ey,
-                                                                    b.sy);
+    oz_split_kernel<<<grid_for((long long)g.Mp * g.Kp), 256, 0, s>>>(X, K, g.Kc, g.Kp, g.Mp, kTM,
+                                                                    b.ex, b.sx);
+    oz_split_kernel<<<grid_for((long long)g.Np * g.Kp), 256, 0, s>>>(Y, K, g.Kc, g.Kp, g.Np, kTN,
+                                                                    b.ey, b.sy);
     static std::atomic<bool> configured[256] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!configured[dev & 255].load(std::memory_order_acquire)) {
-        e = cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kGemmSmem);
+        e = cudaFuncSetAttribute(oz_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTcSmem);
         if (e != cudaSuccess) return e;
         configured[dev & 255].store(true, std::memory_order_release);
     }
-    dim3 grid((unsigned)(g.Mp / kBM), (unsigned)(g.Np / kBN), (unsigned)g.splits);
-    oz_gemm_kernel<<<grid, kThreads, kGemmSmem, s>>>(b.sx, b.sy, g.Mp, g.Np, g.Kp, g.Kc, g.cps,
-                                                     g.nch, b.fold);
+    dim3 grid((unsigned)(g.Mp / kTM), (unsigned)(g.Np / kTN), (unsigned)g.splits);
+    oz_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(b.sx, b.sy, g.Mp, g.Np, g.Kp, g.Kc, g.cps, g.nch,
+                                                   b.fold, err);
     oz_combine_kernel<<<grid_for((long long)g.splits * M * N), 256, 0, s>>>(
         b.fold, b.ex, b.ey, b.exmax, b.eymax, M, N, g.Mp, g.Np, g.cps, g.nch, g.splits, Out,
         out_ld, split_stride);

@@ -28,9 +28,10 @@ int ozaki_splits(int K, int splits);
 // X(m, k) Y(n, k), complex, for m < M, n < N: the k range cut into `splits`
 // contiguous parts (as zgemm3m_kernel cuts it, so split partials can be
 // added in split order by the caller).  Accuracy is that of an FP64 3M-form
-// GEMM; the products run on the tensor cores.
+// GEMM; the products run on the tensor cores (tcgen05).  A block whose
+// bounded pipeline wait ran out sets kErrPipelineTimeout in *err.
 cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, int K, int splits,
-                        double2 *Out, long long out_ld, long long split_stride, void *ws,
+                        double2 *Out, long long out_ld, long long split_stride, void *ws, int *err,
                         cudaStream_t s);
 
 }  // namespace gpp
