@@ -205,61 +205,65 @@ __global__ void __launch_bounds__(256) oz_emax_kernel(const int *E, int nch, int
     }
 }
 
-// Position of (row l, k) in a slice plane, laid out for the tensor cores:
-// blocks of R rows x kTK k (R = kTM for X, kTN for Y), one block per
-// pipeline stage and so one bulk copy, ordered (row tile, k step); inside a
-// block the no-swizzle K-major core-matrix layout of tcgen05.mma -- core
-// matrices of 8 rows x 16 bytes, stored whole (128 bytes), the 8 k-cores of
-// a row group next to each other (1024 bytes per row group).
-__device__ __forceinline__ size_t tile_offset(int l, int k, int R, int Kp) {
-    const int rt = l / R, r = l % R, ks = k / kTK, kk = k % kTK;
-    return ((size_t)rt * (Kp / kTK) + ks) * ((size_t)R * kTK) +
-           (size_t)(((r >> 3) * (kTK / 8) + (kk >> 3)) * 64 + (r & 7) * 8 + (kk & 7));
-}
+// Slice planes are laid out for the tensor cores: blocks of R rows x kTK k
+// (R = kTM for X, kTN for Y), one block per pipeline stage and so one bulk
+// copy, ordered (row tile, k step); inside a block the no-swizzle K-major
+// core-matrix layout of tcgen05.mma -- core matrices of 8 rows x 16 bytes,
+// stored whole (128 bytes), the 8 k-cores of a row group next to each other
+// (1024 bytes per row group).  In memory order: row tile, k step, row group
+// of 8, k-core, row within the group, k within the core.
 
 // Slices of the three real planes (re, im, re + im): plane (g, i) holds
-// s_(i+1) of plane g at (l, k), at tile_offset(l, k) within it; zero outside
+// s_(i+1) of plane g at (l, k) in that layout; zero outside
 // L x K.  The slices are the balanced base-128 digits of
 // round(x 2^(7 S - e)): s_2..s_S in [-64, 63], s_1 the rest (|s_1| <= 128),
 // so x = 2^e sum_i s_i 2^(-7 i) to within 2^(e - 57).  Integer arithmetic
-// throughout (the FP64 pipe is slow on GB300).  A thread per (l, k), k
-// fastest.
-__global__ void __launch_bounds__(256) oz_split_kernel(OzOperand z, int K, int Kc, int Kp, int Lp,
-                                                       int R, const int *E, __nv_bfloat16 *out) {
-    const long long n = (long long)Lp * Kp;
+// throughout (the FP64 pipe is slow on GB300).  A thread per core-matrix row
+// (8 consecutive k of one row l), threads in the planes' memory order, so
+// each writes one 16-byte chunk per plane and a warp writes 512 contiguous
+// bytes.
+__global__ void __launch_bounds__(256, 2) oz_split_kernel(OzOperand z, int K, int Kc, int Kp,
+                                                          int Lp, int R, const int *E,
+                                                          __nv_bfloat16 *out) {
+    const long long n = (long long)Lp * (Kp / 8);
     const size_t plane = (size_t)Lp * Kp;
+    const int groups = R / 8, ksteps = Kp / kTK;
     for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
          t += (long long)gridDim.x * 256) {
-        const int l = (int)(t / Kp), k = (int)(t % Kp);
-        const size_t at = tile_offset(l, k, R, Kp);
-        double2 v = make_double2(0.0, 0.0);
-        if (l < z.L && k < K) v = operand_at(z, l, k);
-        const int e = E[(size_t)(k / Kc) * Lp + l];
-        const double r[3] = {v.x, v.y, v.x + v.y};
+        const int r_lo = (int)(t & 7), j = (int)((t >> 3) & 7);
+        const long long q = t >> 6;
+        const int rg = (int)(q % groups);
+        const long long block = q / groups;
+        const int ks = (int)(block % ksteps), rt = (int)(block / ksteps);
+        const int l = rt * R + rg * 8 + r_lo, k0 = ks * kTK + j * 8;
+        const int e = E[(size_t)(k0 / Kc) * Lp + l];  // one chunk: Kc is a multiple of kTK
+        double2 v[8];
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk)
+            v[kk] = (l < z.L && k0 + kk < K) ? operand_at(z, l, k0 + kk) : make_double2(0.0, 0.0);
 #pragma unroll
         for (int g = 0; g < 3; ++g) {
-            int d[kS];
-            oz_slices(r[g], e, d);
+            unsigned packed[kS][4];
+#pragma unroll
+            for (int kk = 0; kk < 8; ++kk) {
+                const double x = g == 0 ? v[kk].x : g == 1 ? v[kk].y : v[kk].x + v[kk].y;
+                int d[kS];
+                oz_slices(x, e, d);
+#pragma unroll
+                for (int i = 0; i < kS; ++i) {
+                    const unsigned short h = __bfloat16_as_ushort(__int2bfloat16_rn(d[i]));
+                    if (kk & 1)
+                        packed[i][kk >> 1] |= (unsigned)h << 16;
+                    else
+                        packed[i][kk >> 1] = h;
+                }
+            }
 #pragma unroll
             for (int i = 0; i < kS; ++i)
-                out[(size_t)(g * kS + i) * plane + at] = __int2bfloat16_rn(d[i]);
+                *reinterpret_cast<uint4 *>(out + (size_t)(g * kS + i) * plane + (size_t)t * 8) =
+                    make_uint4(packed[i][0], packed[i][1], packed[i][2], packed[i][3]);
         }
     }
-}
-
-// 2^e as a float for e >= -126 (exact), 0 below (a group that far below the
-// largest products is under the float-float resolution).
-__device__ __forceinline__ float pow2f(int e) {
-    return e < -126 ? 0.0f : __int_as_float((e + 127) << 23);
-}
-
-// (h, l) += v in float-float (TwoSum, Knuth); v is exact.
-__device__ __forceinline__ void df_acc(float &h, float &l, float v) {
-    const float s = __fadd_rn(h, v);
-    const float bb = __fsub_rn(s, h);
-    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-    l = __fadd_rn(l, e);
-    h = s;
 }
 
 // ---------------------------------------------------------------------------
@@ -535,43 +539,82 @@ oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restri
     }
 }
 
+// 2^e as a float for e >= -126 (exact), 0 below (a group that far below the
+// largest products is under the float-float resolution).
+__device__ __forceinline__ float pow2f(int e) {
+    return e < -126 ? 0.0f : __int_as_float((e + 127) << 23);
+}
+
+// (h, l) += v in float-float (TwoSum, Knuth); v is exact.
+__device__ __forceinline__ void df_acc(float &h, float &l, float v) {
+    const float s = __fadd_rn(h, v);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    l = __fadd_rn(l, e);
+    h = s;
+}
+
 // Out = (P1 - P2, P3 - P1 - P2) 2^(Emax_x[m] + Emax_y[n]) per split: each
 // plane's group sums scaled by 2^(e_x - Emax_x + e_y - Emax_y - 7 d) for
 // their chunk and added in float-float, in a fixed order; the three planes
-// combined in FP64.
+// combined in FP64.  A thread per (split, row, 4 consecutive columns): the
+// stored sums are read as float4 (the padded columns up to Np hold zeros)
+// and only columns below N are written.
 __global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, const int *EX,
                                                          const int *EY, const int *EXmax,
                                                          const int *EYmax, int M, int N, int Mp,
                                                          int Np, int cps, int nch, int splits,
                                                          double2 *Out, long long out_ld,
                                                          long long split_stride) {
-    const long long n = (long long)splits * M * N;
+    const int quads = (N + 3) / 4;
+    const long long n = (long long)splits * M * quads;
     const size_t fplane = (size_t)Mp * Np;
     for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
          t += (long long)gridDim.x * 256) {
-        const int col = (int)(t % N);
-        const long long q = t / N;
+        const int col0 = (int)(t % quads) * 4;
+        const long long q = t / quads;
         const int row = (int)(q % M), z = (int)(q / M);
         const int c0 = z * cps, nch_here = min(cps, nch - c0);
-        const int exm = __ldg(EXmax + row), eyn = __ldg(EYmax + col);
-        double P[3];
+        const int exm = __ldg(EXmax + row);
+        int eyn[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) eyn[j] = __ldg(EYmax + col0 + j);
+        double P[3][4];
+#pragma unroll
         for (int g = 0; g < 3; ++g) {
-            float h = 0.f, l = 0.f;
+            float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
             for (int cl = 0; cl < nch_here; ++cl) {
                 const int c = c0 + cl;
-                const int sh = __ldg(EX + (size_t)c * Mp + row) - exm +
-                               __ldg(EY + (size_t)c * Np + col) - eyn;
+                const int shx = __ldg(EX + (size_t)c * Mp + row) - exm;
+                int sh[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    sh[j] = shx + __ldg(EY + (size_t)c * Np + col0 + j) - eyn[j];
                 const float *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kGroups) * fplane +
-                                 (size_t)row * Np + col;
+                                 (size_t)row * Np + col0;
+                float4 v[kGroups];
 #pragma unroll
                 for (int grp = 0; grp < kGroups; ++grp)
-                    df_acc(h, l, __ldg(f + grp * fplane) * pow2f(sh - 7 * kGroupD[grp]));
+                    v[grp] = __ldg(reinterpret_cast<const float4 *>(f + grp * fplane));
+#pragma unroll
+                for (int grp = 0; grp < kGroups; ++grp) {
+                    const int d7 = 7 * kGroupD[grp];
+                    df_acc(h[0], l[0], v[grp].x * pow2f(sh[0] - d7));
+                    df_acc(h[1], l[1], v[grp].y * pow2f(sh[1] - d7));
+                    df_acc(h[2], l[2], v[grp].z * pow2f(sh[2] - d7));
+                    df_acc(h[3], l[3], v[grp].w * pow2f(sh[3] - d7));
+                }
             }
-            P[g] = (double)h + (double)l;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) P[g][j] = (double)h[j] + (double)l[j];
         }
-        const int e = exm + eyn;
-        Out[z * split_stride + (long long)row * out_ld + col] =
-            make_double2(scalbn(P[0] - P[1], e), scalbn(P[2] - P[0] - P[1], e));
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (col0 + j >= N) break;
+            const int e = exm + eyn[j];
+            Out[z * split_stride + (long long)row * out_ld + col0 + j] =
+                make_double2(scalbn(P[0][j] - P[1][j], e), scalbn(P[2][j] - P[0][j] - P[1][j], e));
+        }
     }
 }
 
@@ -612,10 +655,10 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
         Y, K, g.Kc, g.nch, g.Np, b.ey);
     oz_emax_kernel<<<grid_for(g.Mp), 256, 0, s>>>(b.ex, g.nch, g.Mp, b.exmax);
     oz_emax_kernel<<<grid_for(g.Np), 256, 0, s>>>(b.ey, g.nch, g.Np, b.eymax);
-    oz_split_kernel<<<grid_for((long long)g.Mp * g.Kp), 256, 0, s>>>(X, K, g.Kc, g.Kp, g.Mp, kTM,
-                                                                    b.ex, b.sx);
-    oz_split_kernel<<<grid_for((long long)g.Np * g.Kp), 256, 0, s>>>(Y, K, g.Kc, g.Kp, g.Np, kTN,
-                                                                    b.ey, b.sy);
+    oz_split_kernel<<<grid_for((long long)g.Mp * g.Kp / 8), 256, 0, s>>>(X, K, g.Kc, g.Kp, g.Mp,
+                                                                        kTM, b.ex, b.sx);
+    oz_split_kernel<<<grid_for((long long)g.Np * g.Kp / 8), 256, 0, s>>>(Y, K, g.Kc, g.Kp, g.Np,
+                                                                        kTN, b.ey, b.sy);
     static std::atomic<bool> configured[256] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -629,7 +672,7 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
     dim3 grid((unsigned)(g.Mp / kTM), (unsigned)(g.Np / kTN), (unsigned)g.splits);
     oz_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(b.sx, b.sy, g.Mp, g.Np, g.Kp, g.Kc, g.cps, g.nch,
                                                    b.fold, err);
-    oz_combine_kernel<<<grid_for((long long)g.splits * M * N), 256, 0, s>>>(
+    oz_combine_kernel<<<grid_for((long long)g.splits * M * ceil_div(N, 4)), 256, 0, s>>>(
         b.fold, b.ex, b.ey, b.exmax, b.eymax, M, N, g.Mp, g.Np, g.cps, g.nch, g.splits, Out,
         out_ld, split_stride);
     count_launch(8);
