@@ -277,6 +277,58 @@ def run_reference(args, shape: W.Shape) -> dict:
     return line if line is not None else run_reference_port(args, shape)
 
 
+def band_independent_leg(d, shape: W.Shape, steps: int) -> dict:
+    """The drop-in entry points' case on the same inputs: band 0's frequencies
+    for every band (the reference's wx_array[3]), so the unoccupied bands go
+    through the band-sum GEMM on the tensor cores.  Per-call device time
+    (CUDA events) in both precisions, with and without the per-band output,
+    and the error of each against the per-term FP64 kernel."""
+    import torch
+    from gppsigma import ops
+    lib = capi.load()
+    dbi = dataclasses.replace(d, wx_array=d.wx_array.reshape(-1, shape.nw)[:1].contiguous(),
+                              wx_stride=0)
+    stream = torch.cuda.current_stream()
+
+    def run(precision: str, n1: bool):
+        out = ops.sigma(dbi, precision, acht_n1=n1)
+        for _ in range(2):
+            ops.sigma(dbi, precision, acht_n1=n1, out=out)
+        ops.wait()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ops.sigma(dbi, precision, acht_n1=n1, out=out)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ops.wait()
+        return out.achtemp.cpu().numpy(), e0.elapsed_time(e1) / steps
+
+    legs, outs = {}, {}
+    for precision in ("fp64", "mixed"):
+        for n1 in (False, True):
+            key = precision + ("_with_per_band_output" if n1 else "")
+            outs[key], ms = run(precision, n1)
+            legs[key] = {"ms_per_call": ms, "terms_per_s": shape.terms / (ms * 1e-3)}
+    capi.check(lib.gpp_set_gemm_path(0), "gpp_set_gemm_path")
+    try:
+        want = ops.sigma(dbi, "fp64")
+        ops.wait()
+        want = want.achtemp.cpu().numpy()
+    finally:
+        capi.check(lib.gpp_set_gemm_path(-1), "gpp_set_gemm_path")
+    w2 = np.concatenate([want.real, want.imag])
+    for key, got in outs.items():
+        g2 = np.concatenate([got.real, got.imag])
+        legs[key]["achtemp_max_rel_err_vs_per_term_fp64"] = float(
+            np.max(np.abs(g2 - w2) / np.where(w2 == 0, 1.0, np.abs(w2))))
+    return {"wx": "band 0's frequencies for every band (the reference's wx_array[3])",
+            "band_sum": "tcgen05 tensor-core GEMM, operands cut into exact bf16 integer slices",
+            "steps": steps, **legs}
+
+
 def shape_dict(s: W.Shape) -> dict:
     return {"number_bands": s.number_bands, "nvband": s.nvband, "ncouls": s.ncouls,
             "ngpown": s.ngpown, "nw": s.nw, "near_pole_fraction": s.near_pole,
@@ -394,6 +446,9 @@ def main() -> int:
     ap.add_argument("--ref-seconds", type=float, default=4.0,
                     help="CPU seconds per step of the reference arm's band sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bi-steps", type=int, default=5,
+                    help="timed calls per leg of the band-independent-frequency report "
+                         "(0: skip it)")
     ap.add_argument("--shard", default="states", choices=["states", "rows"],
                     help="states: one independent state per rank (weak scaling); rows: one "
                          "state split by G' rows across the ranks, partial sums added on "
@@ -626,6 +681,8 @@ def main() -> int:
         line["mixed_speedup_vs_fp64"] = line["value"] / fp64_leg["value"]
     if mixed_vs_oracle:
         line["max_rel_err_vs_oracle"] = mixed_vs_oracle
+    if rank == 0 and args.bi_steps > 0 and args.shard == "states":
+        line["band_independent_wx"] = band_independent_leg(d, shape, args.bi_steps)
     if not args.no_cpu_baseline:
         ref_args = argparse.Namespace(**vars(args))
         ref_args.steps, ref_args.warmup = 1, 0
