@@ -284,7 +284,7 @@ def band_independent_leg(d, shape: W.Shape, steps: int) -> dict:
     (CUDA events) in both precisions, with and without the per-band output,
     and the error of each against the per-term FP64 kernel."""
     import torch
-    from gppsigma import ops
+    from gppsigma import capi, ops
     lib = capi.load()
     dbi = dataclasses.replace(d, wx_array=d.wx_array.reshape(-1, shape.nw)[:1].contiguous(),
                               wx_stride=0)

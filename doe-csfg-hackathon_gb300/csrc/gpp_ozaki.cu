@@ -42,6 +42,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 
 #include "gpp_kernels.h"
 #include "gpp_ozaki.h"
@@ -82,7 +83,17 @@ struct Geometry {
     int Mp, Np;        // padded to the block tile
     int nch, Kc, Kp;   // chunks, chunk length (multiple of kTK), padded K = nch * Kc
     int cps, splits;   // chunks per split, splits
+    int slab_tiles;    // row tiles of X per pass (bounds the stored group sums)
 };
+
+// The stored group sums of one pass take at most 8 GB (GPP_OZAKI_FOLD_MB
+// overrides it, for tests); a larger product runs in passes over slabs of
+// X's row tiles.
+size_t fold_budget() {
+    const char *v = getenv("GPP_OZAKI_FOLD_MB");
+    const long long mb = v ? atoll(v) : 0;
+    return mb > 0 ? (size_t)mb << 20 : size_t(8) << 30;
+}
 
 Geometry geometry(int M, int N, int K, int splits) {
     Geometry g;
@@ -96,6 +107,8 @@ Geometry geometry(int M, int N, int K, int splits) {
     g.Kp = g.nch * g.Kc;
     g.cps = ceil_div(g.nch, std::max(1, splits));
     g.splits = ceil_div(g.nch, g.cps);
+    const size_t per_tile = sizeof(float) * (size_t)g.splits * 3 * g.cps * kGroups * kTM * g.Np;
+    g.slab_tiles = (int)std::max<size_t>(1, std::min<size_t>(g.Mp / kTM, fold_budget() / per_tile));
     return g;
 }
 
@@ -104,11 +117,11 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 struct Buffers {
     __nv_bfloat16 *sx, *sy;
     int *ex, *ey, *exmax, *eymax;
-    float *fold;  // [splits][3][cps][kGroups][Mp][Np]: each group's exact integer sum
+    float *fold;  // [splits][3][cps][kGroups][slab rows][Np]: each group's exact integer sum
 };
 
 size_t fold_elems(const Geometry &g) {
-    return (size_t)g.splits * 3 * g.cps * kGroups * g.Mp * g.Np;
+    return (size_t)g.splits * 3 * g.cps * kGroups * ((size_t)g.slab_tiles * kTM) * g.Np;
 }
 
 Buffers carve(const Geometry &g, void *ws) {
@@ -381,8 +394,9 @@ __device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
 }
 
 // The tensor-core products on tcgen05: block (bx, by, z) computes rows
-// [128 bx, +128) of X against rows [256 by, +256) of Y over split z's
-// chunks.  Warp 0 (one thread) streams each step's two operand blocks into a
+// [128 (mt0 + bx), +128) of X against rows [256 by, +256) of Y over split
+// z's chunks, its group sums stored at slab row 128 bx + ... (slab of Ms
+// rows).  Warp 0 (one thread) streams each step's two operand blocks into a
 // four-stage shared-memory ring with 1-D bulk copies completing on full[s];
 // warp 1 (one thread) issues four K = 16 tcgen05.mma per step into one of two
 // TMEM accumulators (128 lanes x 256 FP32 columns each) and commits to
@@ -394,7 +408,8 @@ __device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
 // copies and MMAs finish and frees its TMEM.
 __global__ void __launch_bounds__(kTcThreads, 1)
 oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restrict__ SY, int Mp,
-             int Np, int Kp, int Kc, int cps, int nch, float *__restrict__ fold, int *err) {
+             int Np, int Kp, int Kc, int cps, int nch, int mt0, int Ms, float *__restrict__ fold,
+             int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sA = smem;
     unsigned char *sB = smem + (size_t)kTStages * kStageA;
@@ -408,7 +423,7 @@ oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restri
     volatile int *abort = abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
+    const int mt = mt0 + blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
     const int c0 = z * cps, nch_here = min(cps, nch - c0);
     const int KS = Kc / kTK, ksteps = Kp / kTK;
     const int T = 3 * nch_here * kPairs * KS;
@@ -487,8 +502,8 @@ oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restri
         }
     } else {  // epilogue: warps 2-5, TMEM lanes 32 (warp % 4) ..
         const int quarter = warp & 3;
-        const int m = mt * kTM + quarter * 32 + lane;
-        const size_t fplane = (size_t)Mp * Np;
+        const int m = blockIdx.x * kTM + quarter * 32 + lane;  // row within the slab
+        const size_t fplane = (size_t)Ms * Np;
         for (int G = 0; G < NG; ++G) {
             const int a = G & 1;
             if (!bar_wait(&accfull[a], (G >> 1) & 1, abort)) break;
@@ -562,18 +577,20 @@ __device__ __forceinline__ void df_acc(float &h, float &l, float v) {
 // and only columns below N are written.
 __global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, const int *EX,
                                                          const int *EY, const int *EXmax,
-                                                         const int *EYmax, int M, int N, int Mp,
-                                                         int Np, int cps, int nch, int splits,
-                                                         double2 *Out, long long out_ld,
+                                                         const int *EYmax, int row0, int rows,
+                                                         int Ms, int N, int Mp, int Np, int cps,
+                                                         int nch, int splits, double2 *Out,
+                                                         long long out_ld,
                                                          long long split_stride) {
     const int quads = (N + 3) / 4;
-    const long long n = (long long)splits * M * quads;
-    const size_t fplane = (size_t)Mp * Np;
+    const long long n = (long long)splits * rows * quads;
+    const size_t fplane = (size_t)Ms * Np;
     for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
          t += (long long)gridDim.x * 256) {
         const int col0 = (int)(t % quads) * 4;
         const long long q = t / quads;
-        const int row = (int)(q % M), z = (int)(q / M);
+        const int r = (int)(q % rows), z = (int)(q / rows);  // slab row
+        const int row = row0 + r;
         const int c0 = z * cps, nch_here = min(cps, nch - c0);
         const int exm = __ldg(EXmax + row);
         int eyn[4];
@@ -591,7 +608,7 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, cons
                 for (int j = 0; j < 4; ++j)
                     sh[j] = shx + __ldg(EY + (size_t)c * Np + col0 + j) - eyn[j];
                 const float *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kGroups) * fplane +
-                                 (size_t)row * Np + col0;
+                                 (size_t)r * Np + col0;
                 float4 v[kGroups];
 #pragma unroll
                 for (int grp = 0; grp < kGroups; ++grp)
@@ -669,13 +686,23 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
         if (e != cudaSuccess) return e;
         configured[dev & 255].store(true, std::memory_order_release);
     }
-    dim3 grid((unsigned)(g.Mp / kTM), (unsigned)(g.Np / kTN), (unsigned)g.splits);
-    oz_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(b.sx, b.sy, g.Mp, g.Np, g.Kp, g.Kc, g.cps, g.nch,
-                                                   b.fold, err);
-    oz_combine_kernel<<<grid_for((long long)g.splits * M * ceil_div(N, 4)), 256, 0, s>>>(
-        b.fold, b.ex, b.ey, b.exmax, b.eymax, M, N, g.Mp, g.Np, g.cps, g.nch, g.splits, Out,
-        out_ld, split_stride);
-    count_launch(8);
+    // Passes over slabs of X's row tiles, each storing its group sums in the
+    // same buffer and combining them into its rows of Out.
+    const int mtiles = g.Mp / kTM, Ms = g.slab_tiles * kTM;
+    int passes = 0;
+    for (int mt0 = 0; mt0 < mtiles; mt0 += g.slab_tiles, ++passes) {
+        const int tiles = std::min(g.slab_tiles, mtiles - mt0);
+        const int row0 = mt0 * kTM, rows = std::min(M - row0, tiles * kTM);
+        dim3 grid((unsigned)tiles, (unsigned)(g.Np / kTN), (unsigned)g.splits);
+        oz_tc_kernel<<<grid, kTcThreads, kTcSmem, s>>>(b.sx, b.sy, g.Mp, g.Np, g.Kp, g.Kc, g.cps,
+                                                       g.nch, mt0, Ms, b.fold, err);
+        if (rows > 0)
+            oz_combine_kernel<<<grid_for((long long)g.splits * rows * ceil_div(N, 4)), 256, 0,
+                                s>>>(b.fold, b.ex, b.ey, b.exmax, b.eymax, row0, rows, Ms, N,
+                                     g.Mp, g.Np, g.cps, g.nch, g.splits, Out, out_ld,
+                                     split_stride);
+    }
+    count_launch(6 + 2 * passes);
     return cudaGetLastError();
 }
 
