@@ -150,6 +150,9 @@ __device__ __forceinline__ double2 operand_at(const OzOperand &z, int l, int k) 
 // Exponent of an all-zero chunk: far enough below any double's that every
 // scale formed from it underflows to zero.
 constexpr int kZeroExp = -4000;
+// Exponent of a chunk holding an Inf or a NaN: its slices are all zero and
+// every output of its row or column becomes NaN in the combining pass.
+constexpr int kNonFiniteExp = 1 << 20;
 
 // |x| as its bit pattern (monotone in |x| for every double but NaN).
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
@@ -162,6 +165,7 @@ __device__ __forceinline__ unsigned long long max3_bits(double2 v) {
 __device__ __forceinline__ int exp_of_bits(unsigned long long b) {
     if (b == 0) return kZeroExp;
     const int E = (int)(b >> 52);
+    if (E == 0x7FF) return kNonFiniteExp;  // the bit patterns of Inf and NaN are the largest
     return E > 0 ? E - 1022 : (63 - __clzll((long long)b)) - 1073;
 }
 
@@ -629,8 +633,11 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, cons
         for (int j = 0; j < 4; ++j) {
             if (col0 + j >= N) break;
             const int e = exm + eyn[j];
-            Out[z * split_stride + (long long)row * out_ld + col0 + j] =
-                make_double2(scalbn(P[0][j] - P[1][j], e), scalbn(P[2][j] - P[0][j] - P[1][j], e));
+            double2 o = make_double2(scalbn(P[0][j] - P[1][j], e), scalbn(P[2][j] - P[0][j] - P[1][j], e));
+            if (exm >= kNonFiniteExp || eyn[j] >= kNonFiniteExp)
+                o = make_double2(__longlong_as_double(0x7FF8000000000000ll),
+                                 __longlong_as_double(0x7FF8000000000000ll));
+            Out[z * split_stride + (long long)row * out_ld + col0 + j] = o;
         }
     }
 }

@@ -4,7 +4,8 @@ operands in both layouts (k contiguous or rows contiguous), with ragged
 sizes, several k chunks and k splits, a wide dynamic range along k, and
 operands whose slices take the extreme values (s_1 = 128, s_2..s_8 = -64:
 the group sums reach 2^23, where FP32 accumulation must still be exact), and
-compares with sums in long double.  The bound is 1e-13 of the largest
+compares with sums in long double; an Inf or NaN input turns its row's or
+column's results into NaN and leaves the others alone.  The bound is 1e-13 of the largest
 result, normwise (an FP64 3M-form GEMM is ~1e-15 to 1e-14 here); the
 device fault word must stay clear.
 """
@@ -111,8 +112,55 @@ static int run(int M, int N, int K, int splits, bool kfast, double range, bool e
     return (rel <= 1e-13 && herr == 0) ? 0 : 1;
 }
 
+// An Inf in row 3 of X and a NaN in row 5 of Y: the results of that row and
+// that column are NaN, every other result as without them.
+static int run_nonfinite() {
+    const int M = 40, N = 70, K = 600;
+    std::vector<double2> X((size_t)K * M), Y((size_t)K * N);
+    for (auto &v : X) v = make_double2(uni() - 0.5, uni() - 0.5);
+    for (auto &v : Y) v = make_double2(uni() - 0.5, uni() - 0.5);
+    std::vector<double2> Xc = X, Yc = Y;  // k-major: X[k * M + m]
+    X[(size_t)550 * M + 3].x = INFINITY;
+    Y[(size_t)7 * N + 5].y = NAN;
+    const int zs = gpp::ozaki_splits(K, 1);
+    double2 *dX, *dY, *dO, *dOc;
+    void *ws;
+    int *derr;
+    if (cudaMalloc(&dX, X.size() * 16) || cudaMalloc(&dY, Y.size() * 16) ||
+        cudaMalloc(&dO, (size_t)zs * M * N * 16) || cudaMalloc(&dOc, (size_t)zs * M * N * 16) ||
+        cudaMalloc(&ws, gpp::ozaki_bytes(M, N, K, 1)) || cudaMalloc(&derr, 4))
+        return 3;
+    cudaMemset(derr, 0, 4);
+    const gpp::OzOperand ox{dX, M, false, M}, oy{dY, N, false, N};
+    cudaMemcpy(dX, X.data(), X.size() * 16, cudaMemcpyHostToDevice);
+    cudaMemcpy(dY, Y.data(), Y.size() * 16, cudaMemcpyHostToDevice);
+    gpp::ozaki_zgemm(ox, oy, M, N, K, 1, dO, N, (long long)M * N, ws, derr, 0);
+    cudaMemcpy(dX, Xc.data(), X.size() * 16, cudaMemcpyHostToDevice);
+    cudaMemcpy(dY, Yc.data(), Y.size() * 16, cudaMemcpyHostToDevice);
+    gpp::ozaki_zgemm(ox, oy, M, N, K, 1, dOc, N, (long long)M * N, ws, derr, 0);
+    if (cudaDeviceSynchronize() != cudaSuccess) return 4;
+    std::vector<double2> O((size_t)M * N), Oc((size_t)M * N);
+    cudaMemcpy(O.data(), dO, O.size() * 16, cudaMemcpyDeviceToHost);
+    cudaMemcpy(Oc.data(), dOc, Oc.size() * 16, cudaMemcpyDeviceToHost);
+    int bad = 0;
+    for (int m = 0; m < M; ++m)
+        for (int n = 0; n < N; ++n) {
+            const double2 o = O[(size_t)m * N + n], c = Oc[(size_t)m * N + n];
+            if (m == 3 || n == 5) {
+                if (!(std::isnan(o.x) && std::isnan(o.y))) ++bad;
+            } else if (std::fabs(o.x - c.x) > 1e-12 * std::fabs(c.x) + 1e-300 ||
+                       std::fabs(o.y - c.y) > 1e-12 * std::fabs(c.y) + 1e-300) {
+                ++bad;
+            }
+        }
+    printf("non-finite inputs: %d wrong results\n", bad);
+    cudaFree(dX); cudaFree(dY); cudaFree(dO); cudaFree(dOc); cudaFree(ws); cudaFree(derr);
+    return bad ? 1 : 0;
+}
+
 int main() {
     int bad = 0;
+    bad |= run_nonfinite();
     bad |= run(37, 300, 510, 1, false, 0, false);
     bad |= run(64, 128, 32, 1, false, 0, false);
     bad |= run(100, 257, 5, 1, true, 0, false);
