@@ -55,6 +55,7 @@ namespace {
 constexpr int kS = kOzSlices;    // slices per operand value
 constexpr int kKcMax = 512;      // k values per chunk (exactness bound)
 constexpr int kGroups = 10;      // fold groups per (plane, chunk)
+constexpr int kSlots = kGroups / 2;  // stored values per (plane, chunk): groups in pairs
 
 // The tensor-core tile: tcgen05.mma M = 128 (rows of X), N = 256 (rows of
 // Y), 64 k per pipeline stage (four K = 16 instructions), four stages.
@@ -75,8 +76,14 @@ __constant__ unsigned char kPairJ[kPairs] = {1, 2, 1, 3, 2, 1, 4, 3, 2, 1, 5, 4,
                                              3, 2, 1, 7, 6, 5, 4, 3, 2, 1, 8, 7, 6, 5, 4, 3, 2, 1};
 __constant__ unsigned char kGroupEnd[kPairs] = {1, 0, 1, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0,
                                                 0, 0, 1, 0, 0, 0, 0, 1, 0, 1, 0, 0, 0, 0, 1, 0, 0, 1};
-// i + j of each group.
-__constant__ unsigned char kGroupD[kGroups] = {2, 3, 4, 5, 6, 7, 8, 8, 9, 9};
+// Groups are stored in pairs (2 s, 2 s + 1) as one exact int32: 128 s_d +
+// s_(d+1) for the pairs of consecutive d (2-3, 4-5, 6-7) and s + s' for the
+// two halves of d = 8 and of d = 9.  Worst cases over 512 k (group bounds
+// 2^23, 2^23; 2^23.3, 2^23.6; 2^23.8, 2^24; and 2^24.2, 2^24.3 for the sums)
+// stay below 2^31.  kSlotD: the d whose scale 2^(-7 d) the packed value
+// carries.
+__constant__ unsigned char kSlotD[kSlots] = {3, 5, 7, 8, 9};
+__constant__ unsigned char kSlotShift[kSlots] = {7, 7, 7, 0, 0};  // log2 of the even group's weight
 
 struct Geometry {
     int M, N, K;       // logical sizes
@@ -107,7 +114,7 @@ Geometry geometry(int M, int N, int K, int splits) {
     g.Kp = g.nch * g.Kc;
     g.cps = ceil_div(g.nch, std::max(1, splits));
     g.splits = ceil_div(g.nch, g.cps);
-    const size_t per_tile = sizeof(float) * (size_t)g.splits * 3 * g.cps * kGroups * kTM * g.Np;
+    const size_t per_tile = sizeof(int) * (size_t)g.splits * 3 * g.cps * kSlots * kTM * g.Np;
     g.slab_tiles = (int)std::max<size_t>(1, std::min<size_t>(g.Mp / kTM, fold_budget() / per_tile));
     return g;
 }
@@ -117,11 +124,11 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 struct Buffers {
     __nv_bfloat16 *sx, *sy;
     int *ex, *ey, *exmax, *eymax;
-    float *fold;  // [splits][3][cps][kGroups][slab rows][Np]: each group's exact integer sum
+    int *fold;  // [splits][3][cps][kSlots][slab rows][Np]: group pairs' exact sums, packed
 };
 
 size_t fold_elems(const Geometry &g) {
-    return (size_t)g.splits * 3 * g.cps * kGroups * ((size_t)g.slab_tiles * kTM) * g.Np;
+    return (size_t)g.splits * 3 * g.cps * kSlots * ((size_t)g.slab_tiles * kTM) * g.Np;
 }
 
 Buffers carve(const Geometry &g, void *ws) {
@@ -139,7 +146,7 @@ Buffers carve(const Geometry &g, void *ws) {
     w += align_up(sizeof(int) * (size_t)g.Mp);
     b.eymax = reinterpret_cast<int *>(w);
     w += align_up(sizeof(int) * (size_t)g.Np);
-    b.fold = reinterpret_cast<float *>(w);
+    b.fold = reinterpret_cast<int *>(w);
     return b;
 }
 
@@ -400,7 +407,7 @@ __device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
 // The tensor-core products on tcgen05: block (bx, by, z) computes rows
 // [128 (mt0 + bx), +128) of X against rows [256 by, +256) of Y over split
 // z's chunks, its group sums stored at slab row 128 bx + ... (slab of Ms
-// rows).  Warp 0 (one thread) streams each step's two operand blocks into a
+// rows), packed in pairs (kSlotD).  Warp 0 (one thread) streams each step's two operand blocks into a
 // four-stage shared-memory ring with 1-D bulk copies completing on full[s];
 // warp 1 (one thread) issues four K = 16 tcgen05.mma per step into one of two
 // TMEM accumulators (128 lanes x 256 FP32 columns each) and commits to
@@ -412,7 +419,7 @@ __device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
 // copies and MMAs finish and frees its TMEM.
 __global__ void __launch_bounds__(kTcThreads, 1)
 oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restrict__ SY, int Mp,
-             int Np, int Kp, int Kc, int cps, int nch, int mt0, int Ms, float *__restrict__ fold,
+             int Np, int Kp, int Kc, int cps, int nch, int mt0, int Ms, int *__restrict__ fold,
              int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *sA = smem;
@@ -514,16 +521,39 @@ oz_tc_kernel(const __nv_bfloat16 *__restrict__ SX, const __nv_bfloat16 *__restri
             tc_fence_after();
             const int grp = G % kGroups, q = G / kGroups;
             const int cl = q % nch_here, g = q / nch_here;
-            float *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kGroups + grp) * fplane +
-                       (size_t)m * Np + (size_t)nt * kTN;
+            const int slot = grp >> 1;
+            int *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kSlots + slot) * fplane +
+                     (size_t)m * Np + (size_t)nt * kTN;
             const unsigned ta = tmem + ((unsigned)(quarter * 32) << 16) + a * kTN;
+            const int shift = kSlotShift[slot];
+            if ((grp & 1) == 0) {  // the even group: its sums as they are
 #pragma unroll 1
-            for (int c = 0; c < kTN; c += 32) {
-                float v[32];
-                tmem_ld32(ta + c, v);
+                for (int c = 0; c < kTN; c += 32) {
+                    float v[32];
+                    tmem_ld32(ta + c, v);
 #pragma unroll
-                for (int j = 0; j < 32; j += 4)
-                    *reinterpret_cast<float4 *>(f + c + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+                    for (int j = 0; j < 32; j += 4)
+                        *reinterpret_cast<int4 *>(f + c + j) =
+                            make_int4(__float2int_rn(v[j]), __float2int_rn(v[j + 1]),
+                                      __float2int_rn(v[j + 2]), __float2int_rn(v[j + 3]));
+                }
+            } else {  // the odd group: packed with the even one this thread stored
+#pragma unroll 1
+                for (int c = 0; c < kTN; c += 32) {
+                    int4 e[8];  // read back before the TMEM load, so that the two overlap
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) e[j] = *reinterpret_cast<const int4 *>(f + c + 4 * j);
+                    float v[32];
+                    tmem_ld32(ta + c, v);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        e[j].x = (e[j].x << shift) + __float2int_rn(v[4 * j]);
+                        e[j].y = (e[j].y << shift) + __float2int_rn(v[4 * j + 1]);
+                        e[j].z = (e[j].z << shift) + __float2int_rn(v[4 * j + 2]);
+                        e[j].w = (e[j].w << shift) + __float2int_rn(v[4 * j + 3]);
+                        *reinterpret_cast<int4 *>(f + c + 4 * j) = e[j];
+                    }
+                }
             }
             tc_fence_before();
             bar_arrive(&accempty[a]);
@@ -573,13 +603,66 @@ __device__ __forceinline__ void df_acc(float &h, float &l, float v) {
     h = s;
 }
 
+// (h, l) = (ah + al) + (bh + bl): the heads by TwoSum, exactly; the tails
+// and the heads' error added in float (about 2^-47 of the larger operand);
+// the pair is left unnormalised for its conversion to a double.
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float &h, float &l) {
+    const float s = __fadd_rn(ah, bh);
+    const float bb = __fsub_rn(s, ah);
+    const float e = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    l = __fadd_rn(__fadd_rn(al, bl), e);
+    h = s;
+}
+
+// A packed group-pair sum v (|v| < 2^31) as two exact floats hi + lo, hi a
+// multiple of 2^16: 2^23 + (v mod 2^16) and 1.5 2^23 + (v >> 16) are built
+// from their bits and the offsets taken off (all exact; no conversion
+// instruction).
+__device__ __forceinline__ void split_packed(int v, float &hi, float &lo) {
+    lo = __fsub_rn(__int_as_float(0x4B000000 | (v & 0xFFFF)), 8388608.0f);
+    hi = __fmul_rn(__fsub_rn(__int_as_float(0x4B400000 + (v >> 16)), 12582912.0f), 65536.0f);
+}
+
+// The double of a float from its bits (exponent rebiased by 1023 - 127, the
+// mantissa moved up 29 bits); subnormal and non-finite floats go through the
+// conversion instruction.  Exact either way.
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ef = (u >> 23) & 0xFFu;
+    if ((u & 0x7FFFFFFFu) == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
+    if (ef == 0 || ef == 0xFFu) return (double)x;
+    return __hiloint2double((int)((u & 0x80000000u) | ((ef + 896u) << 20) | ((u >> 3) & 0xFFFFFu)),
+                            (int)(u << 29));
+}
+
+// d 2^e: the exponent field moved when d and the result are normal doubles
+// (exact, as scalbn is), scalbn otherwise.
+__device__ __forceinline__ double scale2(double d, int e) {
+    const int hi = __double2hiint(d);
+    const int ed = (hi >> 20) & 0x7FF;
+    if (ed != 0 && ed != 0x7FF && ed + e >= 1 && ed + e <= 2046)
+        return __hiloint2double(hi + (e << 20), __double2loint(d));
+    return scalbn(d, e);
+}
+
+// The (4 columns, slab row, split) of flat index t.
+template <typename I>
+__device__ __forceinline__ void combine_cell(I t, I quads, I rows, int &col0, int &r, int &z) {
+    col0 = (int)(t % quads) * 4;
+    const I q = t / quads;
+    r = (int)(q % rows);
+    z = (int)(q / rows);
+}
+
 // Out = (P1 - P2, P3 - P1 - P2) 2^(Emax_x[m] + Emax_y[n]) per split: each
-// plane's group sums scaled by 2^(e_x - Emax_x + e_y - Emax_y - 7 d) for
-// their chunk and added in float-float, in a fixed order; the three planes
-// combined in FP64.  A thread per (split, row, 4 consecutive columns): the
-// stored sums are read as float4 (the padded columns up to Np hold zeros)
+// plane's packed group sums (split into two exact floats) scaled by
+// 2^(e_x - Emax_x + e_y - Emax_y - 7 d) for their chunk and added in
+// float-float, in a fixed order; the three planes combined in float-float
+// and each result converted to FP64 (two FP64 adds per result: the FP64 pipe
+// is the scarce one).  A thread per (split, row, 4 consecutive columns): the
+// stored sums are read as int4 (the padded columns up to Np hold zeros)
 // and only columns below N are written.
-__global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, const int *EX,
+__global__ void __launch_bounds__(256) oz_combine_kernel(const int *fold, const int *EX,
                                                          const int *EY, const int *EXmax,
                                                          const int *EYmax, int row0, int rows,
                                                          int Ms, int N, int Mp, int Np, int cps,
@@ -588,52 +671,65 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(const float *fold, cons
                                                          long long split_stride) {
     const int quads = (N + 3) / 4;
     const long long n = (long long)splits * rows * quads;
+    const bool n32 = n < (1ll << 31);  // 32-bit index arithmetic when it fits
     const size_t fplane = (size_t)Ms * Np;
     for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n;
          t += (long long)gridDim.x * 256) {
-        const int col0 = (int)(t % quads) * 4;
-        const long long q = t / quads;
-        const int r = (int)(q % rows), z = (int)(q / rows);  // slab row
+        int col0, r, z;  // r: slab row
+        if (n32)
+            combine_cell<unsigned>((unsigned)t, (unsigned)quads, (unsigned)rows, col0, r, z);
+        else
+            combine_cell<long long>(t, quads, rows, col0, r, z);
         const int row = row0 + r;
         const int c0 = z * cps, nch_here = min(cps, nch - c0);
         const int exm = __ldg(EXmax + row);
         int eyn[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) eyn[j] = __ldg(EYmax + col0 + j);
-        double P[3][4];
+        // Each plane's float-float sums: chunk by chunk, slot by slot, the same
+        // order for every plane; a chunk's 15 loads are issued together.
+        float PH[3][4] = {}, PL[3][4] = {};
+        for (int cl = 0; cl < nch_here; ++cl) {
+            const int c = c0 + cl;
+            const int shx = __ldg(EX + (size_t)c * Mp + row) - exm;
+            int sh[4];
 #pragma unroll
-        for (int g = 0; g < 3; ++g) {
-            float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int cl = 0; cl < nch_here; ++cl) {
-                const int c = c0 + cl;
-                const int shx = __ldg(EX + (size_t)c * Mp + row) - exm;
-                int sh[4];
+            for (int j = 0; j < 4; ++j) sh[j] = shx + __ldg(EY + (size_t)c * Np + col0 + j) - eyn[j];
+            const int *f = fold + (((size_t)z * 3 * cps + cl) * kSlots) * fplane + (size_t)r * Np + col0;
+            int4 v[3][kSlots];
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    sh[j] = shx + __ldg(EY + (size_t)c * Np + col0 + j) - eyn[j];
-                const float *f = fold + ((((size_t)z * 3 + g) * cps + cl) * kGroups) * fplane +
-                                 (size_t)r * Np + col0;
-                float4 v[kGroups];
+            for (int g = 0; g < 3; ++g)
 #pragma unroll
-                for (int grp = 0; grp < kGroups; ++grp)
-                    v[grp] = __ldg(reinterpret_cast<const float4 *>(f + grp * fplane));
+                for (int sl = 0; sl < kSlots; ++sl)
+                    v[g][sl] = __ldg(reinterpret_cast<const int4 *>(
+                        f + ((size_t)g * cps * kSlots + sl) * fplane));
 #pragma unroll
-                for (int grp = 0; grp < kGroups; ++grp) {
-                    const int d7 = 7 * kGroupD[grp];
-                    df_acc(h[0], l[0], v[grp].x * pow2f(sh[0] - d7));
-                    df_acc(h[1], l[1], v[grp].y * pow2f(sh[1] - d7));
-                    df_acc(h[2], l[2], v[grp].z * pow2f(sh[2] - d7));
-                    df_acc(h[3], l[3], v[grp].w * pow2f(sh[3] - d7));
+            for (int sl = 0; sl < kSlots; ++sl) {
+                const int d7 = 7 * kSlotD[sl];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float sc = pow2f(sh[j] - d7);
+#pragma unroll
+                    for (int g = 0; g < 3; ++g) {
+                        const int vv = j == 0 ? v[g][sl].x : j == 1 ? v[g][sl].y : j == 2 ? v[g][sl].z : v[g][sl].w;
+                        float hi, lo;
+                        split_packed(vv, hi, lo);
+                        df_acc(PH[g][j], PL[g][j], __fmul_rn(hi, sc));
+                        df_acc(PH[g][j], PL[g][j], __fmul_rn(lo, sc));
+                    }
                 }
             }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) P[g][j] = (double)h[j] + (double)l[j];
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             if (col0 + j >= N) break;
             const int e = exm + eyn[j];
-            double2 o = make_double2(scalbn(P[0][j] - P[1][j], e), scalbn(P[2][j] - P[0][j] - P[1][j], e));
+            // The 3M combination in float-float on the FP32 pipe; two FP64 adds per result.
+            float rh, rl, bh, bl, ih, il;
+            df_add(PH[0][j], PL[0][j], -PH[1][j], -PL[1][j], rh, rl);
+            df_add(PH[0][j], PL[0][j], PH[1][j], PL[1][j], bh, bl);
+            df_add(PH[2][j], PL[2][j], -bh, -bl, ih, il);
+            double2 o = make_double2(scale2(f2d(rh) + f2d(rl), e), scale2(f2d(ih) + f2d(il), e));
             if (exm >= kNonFiniteExp || eyn[j] >= kNonFiniteExp)
                 o = make_double2(__longlong_as_double(0x7FF8000000000000ll),
                                  __longlong_as_double(0x7FF8000000000000ll));
@@ -659,7 +755,7 @@ size_t ozaki_bytes(int M, int N, int K, int splits) {
            align_up(sizeof(__nv_bfloat16) * 3 * kS * (size_t)g.Np * g.Kp) +
            align_up(sizeof(int) * (size_t)g.nch * g.Mp) + align_up(sizeof(int) * (size_t)g.nch * g.Np) +
            align_up(sizeof(int) * (size_t)g.Mp) + align_up(sizeof(int) * (size_t)g.Np) +
-           align_up(sizeof(float) * fold_elems(g));
+           align_up(sizeof(int) * fold_elems(g));
 }
 
 int ozaki_splits(int K, int splits) { return geometry(1, 1, K, splits).splits; }

@@ -6,7 +6,8 @@ the slices reconstruct x = 2^e sum_i s_i 2^(-7 i) to within 2^(e - 57)
 in [-64, 63] (the bounds the exact group sums rest on), and every slice is an
 integer that bf16 holds exactly.  The group table of gpp_ozaki.cu is checked
 against those bounds: each group's worst-case sum over 512 k values stays
-within 2^24, where FP32 accumulation is exact.
+within 2^24, where FP32 accumulation is exact, and the groups stored in pairs
+as one integer stay within int32.
 """
 import os
 import re
@@ -98,14 +99,19 @@ def test_slices_reconstruct_and_stay_in_range(tmp_path):
 
 
 def _table(name, text):
-    m = re.search(name + r"\[kPairs\] = \{([^}]*)\}", text) or re.search(name + r"\[kGroups\] = \{([^}]*)\}", text)
+    m = re.search(name + r"\[(?:kPairs|kGroups|kSlots)\] = \{([^}]*)\}", text)
     return [int(v) for v in m.group(1).replace("\n", " ").split(",")]
 
 
-def test_group_table_sums_fit_in_fp32():
+def test_group_table_sums_fit_in_fp32_and_pairs_in_int32():
+    """Each group's worst-case sum over a chunk stays within 2^24 (exact FP32
+    accumulation in tensor memory); the groups stored in pairs as one integer
+    (the even group times 2^shift plus the odd one, scale 2^(-7 d) of the odd
+    group) stay below 2^31, and the combining pass's split of that integer
+    into 128 (v >> 7) and v & 127 gives two floats that hold it exactly."""
     text = open(os.path.join(CSRC, "gpp_ozaki.cu")).read()
     pi, pj, end = _table("kPairI", text), _table("kPairJ", text), _table("kGroupEnd", text)
-    gd = _table("kGroupD", text)
+    slot_d, slot_shift = _table("kSlotD", text), _table("kSlotShift", text)
     kc = int(re.search(r"constexpr int kKcMax = (\d+);", text).group(1))
     bound = lambda i: 128 if i == 1 else 64
     pairs = set(zip(pi, pj))
@@ -118,7 +124,17 @@ def test_group_table_sums_fit_in_fp32():
         if e:
             groups.append(cur)
             cur = []
-    assert not cur and len(groups) == len(gd) == 10
-    for g, d in zip(groups, gd):
-        assert all(i + j == d for i, j in g)
-        assert sum(bound(i) * bound(j) for i, j in g) * kc <= 2 ** 24
+    assert not cur and len(groups) == 10 and len(slot_d) == len(slot_shift) == 5
+    gd, worst = [], []
+    for g in groups:
+        d = {i + j for i, j in g}
+        assert len(d) == 1
+        gd.append(d.pop())
+        worst.append(sum(bound(i) * bound(j) for i, j in g) * kc)
+        assert worst[-1] <= 2 ** 24
+    for s, (d, sh) in enumerate(zip(slot_d, slot_shift)):
+        de, do = gd[2 * s], gd[2 * s + 1]
+        assert do == d and (do - de) * 7 == sh  # the even group's weight relative to the odd
+        packed = (worst[2 * s] << sh) + worst[2 * s + 1]
+        assert packed < 2 ** 31
+        assert (packed >> 7) <= 2 ** 24  # 128 (v >> 7) is an exact float
