@@ -54,16 +54,20 @@ flag_fp64_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
                                           (long long)blockIdx.y * row_tiles + row_tile, red, S);
 }
 
-// Band-independent frequencies: blockIdx.y covers NB occupied bands.
+// Band-independent frequencies: blockIdx.y covers NB occupied bands; a
+// block walks row tiles row_tile0 + blockIdx.x, + gridDim.x, ... below
+// row_tile0 + count.
 template <int RG, int NWC, int NB, int THREADS, int SEM>
 __global__ void __launch_bounds__(THREADS)
-flag_fp64_multi_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
+flag_fp64_multi_kernel(Problem p, Partials part, int row_tile0, int count, int row_tiles) {
     constexpr int K = NB * RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + blockIdx.x,
-                                                    blockIdx.y * NB, blockIdx.z, row_tiles, red,
-                                                    S);
+    for (int t = blockIdx.x; t < count; t += gridDim.x) {
+        flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + t, blockIdx.y * NB,
+                                                        blockIdx.z, row_tiles, red, S);
+        __syncthreads();  // the epilogue has read S before the next tile reduces into it
+    }
 }
 
 // Static term of reduce_achstemp (gppComplex_seq.cpp:66-101): one thread per
@@ -141,36 +145,59 @@ bool flag_multi_enabled() {
     return !(v && v[0] == '0');
 }
 
+// Blocks per SM of the occupied-band pair kernel (0: one block per row
+// tile); GPP_FLAG_BLOCKS_PER_SM, read on every call, overrides the caller's.
+int flag_blocks_per_sm(int asked) {
+    const char *v = getenv("GPP_FLAG_BLOCKS_PER_SM");
+    return v ? atoi(v) : asked;
+}
+
 template <int RG, int NWC, int NB, int THREADS>
 cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles r, int row_tiles,
-                                cudaStream_t s) {
-    dim3 grid(r.end - r.begin, ceil_div(p.nv, NB), ceil_div(p.nw, NWC));
-    if (p.semantics == kSemKerSeq)
+                                int blocks_per_sm, cudaStream_t s) {
+    const int count = r.end - r.begin;
+    dim3 grid(count, ceil_div(p.nv, NB), ceil_div(p.nw, NWC));
+    const int per_sm = flag_blocks_per_sm(blocks_per_sm);
+    if (per_sm > 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long cap = (long long)std::max(sms, 1) * per_sm / ((long long)grid.y * grid.z);
+        grid.x = (unsigned)std::max(1ll, std::min<long long>(count, cap));
+    }
+    if (p.semantics == kSemKerSeq) {
+        prefer_max_shared(flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemKerSeq>);
         flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(
-            p, part, r.begin, row_tiles);
-    else
+            p, part, r.begin, count, row_tiles);
+    } else {
+        prefer_max_shared(flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemComplexSeq>);
         flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(
-            p, part, r.begin, row_tiles);
+            p, part, r.begin, count, row_tiles);
+    }
     count_launch();
     return cudaGetLastError();
 }
 
 template <int RG, int NWC, int THREADS>
-cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, cudaStream_t s) {
+cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, int blocks_per_sm,
+                          cudaStream_t s) {
     const int row_tiles = ceil_div(p.ng, RG);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
     if constexpr (NWC <= 4) {  // two bands of 8 frequencies would spill
         if (p.wx_stride == 0 && p.nv >= 2 && flag_multi_enabled())
-            return launch_flag_multi_t<RG, NWC, 2, THREADS>(p, part, r, row_tiles, s);
+            return launch_flag_multi_t<RG, NWC, 2, THREADS>(p, part, r, row_tiles, blocks_per_sm, s);
     }
     dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
-    if (p.semantics == kSemKerSeq)
+    if (p.semantics == kSemKerSeq) {
+        prefer_max_shared(flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq>);
         flag_fp64_kernel<RG, NWC, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(p, part, r.begin,
                                                                                 row_tiles);
-    else
+    } else {
+        prefer_max_shared(flag_fp64_kernel<RG, NWC, THREADS, kSemComplexSeq>);
         flag_fp64_kernel<RG, NWC, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(
             p, part, r.begin, row_tiles);
+    }
     count_launch();
     return cudaGetLastError();
 }
@@ -200,14 +227,15 @@ cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int b0, i
     }
 }
 
-cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s, RowTiles rt) {
+cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s, RowTiles rt,
+                             int blocks_per_sm) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_flag_t<2, 1, 128>(p, part, rt, s);
-        case 2: return launch_flag_t<2, 2, 128>(p, part, rt, s);
-        case 3: return launch_flag_t<2, 3, 128>(p, part, rt, s);
-        case 4: return launch_flag_t<2, 4, 128>(p, part, rt, s);
-        default: return launch_flag_t<2, 8, 128>(p, part, rt, s);
+        case 1: return launch_flag_t<2, 1, 128>(p, part, rt, blocks_per_sm, s);
+        case 2: return launch_flag_t<2, 2, 128>(p, part, rt, blocks_per_sm, s);
+        case 3: return launch_flag_t<2, 3, 128>(p, part, rt, blocks_per_sm, s);
+        case 4: return launch_flag_t<2, 4, 128>(p, part, rt, blocks_per_sm, s);
+        default: return launch_flag_t<2, 8, 128>(p, part, rt, blocks_per_sm, s);
     }
 }
 

@@ -41,8 +41,11 @@ struct RowTiles {
 cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int band_begin,
                                int band_end, cudaStream_t s, RowTiles rows = RowTiles());
 // Occupied bands [0, nvband): full ssxt_scht_solver branch logic in FP64.
+// blocks_per_sm > 0 (band-independent frequencies only): a persistent grid of
+// that many blocks per SM walking the row tiles, for a launch beside the
+// tensor-core GEMM (GPP_FLAG_BLOCKS_PER_SM overrides it).
 cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s,
-                             RowTiles rows = RowTiles());
+                             RowTiles rows = RowTiles(), int blocks_per_sm = 0);
 // Static term (reduce_achstemp) over all bands: one partial per block.
 int achstemp_blocks(const Problem &p);
 cudaError_t launch_achstemp(const Problem &p, double2 *partials, int *err, cudaStream_t s);
@@ -123,5 +126,17 @@ gpp_status check_grid_limits(const Problem &p, int occupied_bands, int unoccupie
 
 // Per-thread launch counter (gpp_launch_count).
 void count_launch(int n = 1);
+
+// The largest shared-memory carve-out for a kernel that runs beside the
+// tensor-core GEMM (one block of ~193 KB of shared memory per SM): an SM
+// changes its L1/shared split only when no block is resident, so blocks that
+// left it at a small split keep the GEMM's blocks off that SM until they
+// drain.  A hint: a refusal is cleared and ignored.
+template <typename Kernel>
+inline void prefer_max_shared(Kernel *kernel) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+        cudaGetLastError();
+}
 
 }  // namespace gpp

@@ -304,12 +304,15 @@ cudaError_t launch_flag_mixed_t(const Problem &p, const Partials &part, const Sp
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
     dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
-    if (p.semantics == kSemKerSeq)
+    if (p.semantics == kSemKerSeq) {
+        prefer_max_shared(flag_mixed_kernel<2, NWC, 128, kSemKerSeq>);
         flag_mixed_kernel<2, NWC, 128, kSemKerSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
                                                                         row_tiles);
-    else
+    } else {
+        prefer_max_shared(flag_mixed_kernel<2, NWC, 128, kSemComplexSeq>);
         flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
                                                                             row_tiles);
+    }
     count_launch();
     return cudaGetLastError();
 }

@@ -165,8 +165,9 @@ constexpr int kNonFiniteExp = 1 << 20;
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
     return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
+// A bound on |re|, |im|, |re + im| as bits (no FP64 instruction).
 __device__ __forceinline__ unsigned long long max3_bits(double2 v) {
-    return max(max(abs_bits(v.x), abs_bits(v.y)), abs_bits(v.x + v.y));
+    return max(max(abs_bits(v.x), abs_bits(v.y)), oz_sum_abs_bits(v.x, v.y));
 }
 // The e of frexp for the nonzero magnitude with bits b (b < 2^e).
 __device__ __forceinline__ int exp_of_bits(unsigned long long b) {
@@ -270,9 +271,14 @@ __global__ void __launch_bounds__(256, 2) oz_split_kernel(OzOperand z, int K, in
             unsigned packed[kS][4];
 #pragma unroll
             for (int kk = 0; kk < 8; ++kk) {
-                const double x = g == 0 ? v[kk].x : g == 1 ? v[kk].y : v[kk].x + v[kk].y;
+                // re and im as fixed-point integers; the re + im plane is their
+                // sum (within one unit of round((re + im) 2^(56 - e)), at most
+                // 2^56 + 1 in magnitude), formed without an FP64 addition.
+                const long long N = g == 0   ? oz_fixed_point(v[kk].x, e)
+                                    : g == 1 ? oz_fixed_point(v[kk].y, e)
+                                             : oz_fixed_point(v[kk].x, e) + oz_fixed_point(v[kk].y, e);
                 int d[kS];
-                oz_slices(x, e, d);
+                oz_digits(N, d);
 #pragma unroll
                 for (int i = 0; i < kS; ++i) {
                     const unsigned short h = __bfloat16_as_ushort(__int2bfloat16_rn(d[i]));
@@ -623,20 +629,19 @@ __device__ __forceinline__ void split_packed(int v, float &hi, float &lo) {
     hi = __fmul_rn(__fsub_rn(__int_as_float(0x4B400000 + (v >> 16)), 12582912.0f), 65536.0f);
 }
 
-// The double of a float from its bits (exponent rebiased by 1023 - 127, the
-// mantissa moved up 29 bits); subnormal and non-finite floats go through the
-// conversion instruction.  Exact either way.
-__device__ __forceinline__ double f2d(float x) {
-    const unsigned u = __float_as_uint(x);
-    const unsigned ef = (u >> 23) & 0xFFu;
-    if ((u & 0x7FFFFFFFu) == 0) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (ef == 0 || ef == 0xFFu) return (double)x;
-    return __hiloint2double((int)((u & 0x80000000u) | ((ef + 896u) << 20) | ((u >> 3) & 0xFFFFFu)),
-                            (int)(u << 29));
+// The double of a float-float pair: renormalised by TwoSum (exact), then
+// assembled from the bits; FP64 only for a subnormal or non-finite head.
+__device__ __forceinline__ double df_to_double(float h, float l) {
+    const float s = __fadd_rn(h, l);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(l, bb));
+    bool ok;
+    const double d = oz_pair_to_double(s, e, &ok);
+    return ok ? d : (double)s + (double)e;
 }
 
 // d 2^e: the exponent field moved when d and the result are normal doubles
-// (exact, as scalbn is), scalbn otherwise.
+// (exact, as scalbn is), scalbn otherwise (off the common path).
 __device__ __forceinline__ double scale2(double d, int e) {
     const int hi = __double2hiint(d);
     const int ed = (hi >> 20) & 0x7FF;
@@ -658,8 +663,10 @@ __device__ __forceinline__ void combine_cell(I t, I quads, I rows, int &col0, in
 // plane's packed group sums (split into two exact floats) scaled by
 // 2^(e_x - Emax_x + e_y - Emax_y - 7 d) for their chunk and added in
 // float-float, in a fixed order; the three planes combined in float-float
-// and each result converted to FP64 (two FP64 adds per result: the FP64 pipe
-// is the scarce one).  A thread per (split, row, 4 consecutive columns): the
+// and each result assembled into a double from the bits, with no FP64
+// instruction on the common path (the FP64 pipe is the scarce one, and an
+// FP64 instruction stalls this pass beside the FP64 occupied-band kernel).
+// A thread per (split, row, 4 consecutive columns): the
 // stored sums are read as int4 (the padded columns up to Np hold zeros)
 // and only columns below N are written.
 __global__ void __launch_bounds__(256) oz_combine_kernel(const int *fold, const int *EX,
@@ -724,12 +731,12 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(const int *fold, const 
         for (int j = 0; j < 4; ++j) {
             if (col0 + j >= N) break;
             const int e = exm + eyn[j];
-            // The 3M combination in float-float on the FP32 pipe; two FP64 adds per result.
+            // The 3M combination in float-float on the FP32 pipe.
             float rh, rl, bh, bl, ih, il;
             df_add(PH[0][j], PL[0][j], -PH[1][j], -PL[1][j], rh, rl);
             df_add(PH[0][j], PL[0][j], PH[1][j], PL[1][j], bh, bl);
             df_add(PH[2][j], PL[2][j], -bh, -bl, ih, il);
-            double2 o = make_double2(scale2(f2d(rh) + f2d(rl), e), scale2(f2d(ih) + f2d(il), e));
+            double2 o = make_double2(scale2(df_to_double(rh, rl), e), scale2(df_to_double(ih, il), e));
             if (exm >= kNonFiniteExp || eyn[j] >= kNonFiniteExp)
                 o = make_double2(__longlong_as_double(0x7FF8000000000000ll),
                                  __longlong_as_double(0x7FF8000000000000ll));

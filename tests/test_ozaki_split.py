@@ -138,3 +138,102 @@ def test_group_table_sums_fit_in_fp32_and_pairs_in_int32():
         packed = (worst[2 * s] << sh) + worst[2 * s + 1]
         assert packed < 2 ** 31
         assert (packed >> 7) <= 2 ** 24  # 128 (v >> 7) is an exact float
+
+
+HELPERS = r"""
+#include <cfenv>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include "gpp_ozaki_split.cuh"
+
+static unsigned long long st = 77;
+static unsigned long long nx() {
+    unsigned long long z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+static double any_double(int t) {
+    unsigned long long u = nx();
+    double x;
+    switch (t % 5) {
+        case 0: x = ldexp((double)(u >> 11) / 9007199254740992.0, (int)(nx() % 80) - 40); break;
+        case 1: memcpy(&x, &u, 8); if (!std::isfinite(x)) x = 1.5; break;
+        case 2: x = ldexp((double)(u % 1000003), -1074 + (int)(nx() % 60)); break;  // subnormal
+        case 3: x = ldexp(1.0, (int)(nx() % 2046) - 1022); break;                   // powers of two
+        default: x = ldexp(1.0 - ldexp(1.0, -53), 1024 - (int)(nx() % 3)); break;   // near the top
+    }
+    return (nx() & 1) ? -x : x;
+}
+
+int main() {
+    int bad = 0;
+    volatile double vx, vy;
+    for (int t = 0; t < 2000000; ++t) {
+        const double x = any_double(t), y = (t & 8) ? any_double(t / 7) : x * ldexp(1.0, (int)(nx() % 9) - 4);
+        const unsigned long long b = gpp::oz_sum_abs_bits(x, y);
+        vx = fabs(x);
+        vy = fabs(y);
+        if (std::signbit(x) != std::signbit(y)) {
+            if (b != 0) { if (bad++ < 5) printf("opposite signs gave %llx\n", b); }
+            continue;
+        }
+        fesetround(FE_UPWARD);
+        const double up = vx + vy;  // the smallest double >= |x| + |y| (Inf past the top)
+        fesetround(FE_TONEAREST);
+        const double B = gpp::oz_double(b);
+        // B >= the exact sum, so B >= up; and no more than one unit above it
+        if (!(B >= up) || (std::isfinite(up) && B > nextafter(up, INFINITY))) {
+            if (bad++ < 5) printf("x %a y %a: bound %a, sum rounded up %a\n", x, y, B, up);
+        }
+    }
+    for (int t = 0; t < 2000000; ++t) {
+        double v;
+        switch (t % 4) {
+            case 0: v = ldexp((double)(nx() >> 11) / 9007199254740992.0 + 0.5, (int)(nx() % 200) - 100); break;
+            case 1: v = ldexp(1.0, (int)(nx() % 200) - 100) * (1.0 - ldexp((double)(nx() % 64), -40)); break;
+            case 2: v = ldexp(1.0, (int)(nx() % 200) - 100) * (1.0 + ldexp((double)(nx() % 64), -50)); break;
+            default: v = ldexp(1.0, (int)(nx() % 200) - 100); break;
+        }
+        if (nx() & 1) v = -v;
+        const float h = (float)v;
+        const float l = (float)(v - (double)h);  // |l| <= ulp(h) / 2: a normalised pair
+        bool ok = false;
+        const double d = gpp::oz_pair_to_double(h, l, &ok);
+        const long double want = (long double)h + (long double)l;
+        const double ulp = fabs(nextafter((double)want, INFINITY) - (double)want);
+        if (!ok || fabsl((long double)d - want) > ulp) {
+            if (bad++ < 5) printf("h %a l %a: got %a want %La (ok %d)\n", h, l, d, want, (int)ok);
+        }
+    }
+    bool ok = true;
+    const double z = gpp::oz_pair_to_double(-0.0f, 0.0f, &ok);
+    if (!ok || z != 0.0 || !std::signbit(z)) { ++bad; printf("signed zero\n"); }
+    gpp::oz_pair_to_double(1e-40f, 0.0f, &ok);
+    if (ok) { ++bad; printf("subnormal head not refused\n"); }
+    printf("%d failures\n", bad);
+    return bad ? 1 : 0;
+}
+"""
+
+
+def test_fp64_free_helpers_bound_and_assemble(tmp_path):
+    """The bit-level steps that keep FP64 instructions out of the exponent
+    and combining passes: the bound on |x + y| is never below the sum (so no
+    slice overflows) and at most one unit above it rounded up; a normalised
+    float-float pair assembles into a double within one unit in the last
+    place of h + l."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    src = tmp_path / "ozaki_helpers_check.cu"
+    src.write_text(HELPERS)
+    exe = tmp_path / "ozaki_helpers_check"
+    r = subprocess.run([nvcc, "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+                        "-Xcompiler", "-frounding-math", "-I", CSRC, str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "0 failures" in out.stdout
