@@ -297,6 +297,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
     const size_t o_asx = off; off = align_up(off + sizeof(double2) * (size_t)(tiles_f * p.nw));
     const size_t o_n1 = off; off = align_up(off + (want_n1 ? sizeof(double2) * (size_t)(n1_seg * p.nb) : 0));
     const size_t o_st = off; off = align_up(off + sizeof(double2) * (size_t)achs_blocks);
+    const size_t o_next = off; off = align_up(off + sizeof(int));  // work counter
     const size_t o_split = off; off = align_up(off + (mixed ? mixed_split_bytes(p) : 0));
     // Band sums on the tensor cores (both precisions; mixed precision then
     // splits G into its float-float planes) unless gpp_set_gemm_path(2).
@@ -408,7 +409,8 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
             // GEMM's MMAs make no progress while FP64 instructions are in
             // flight on an SM, and a lighter FP64 load leaves them more time.
             e = mixed ? launch_flag_mixed(p, part, w + o_split, side->st)
-                      : launch_flag_fp64(p, part, side->st, RowTiles(), gemm && tensor ? 1 : 0);
+                      : launch_flag_fp64(p, part, side->st, RowTiles(), gemm && tensor ? 1 : 0,
+                                         reinterpret_cast<int *>(w + o_next));
         if (e == cudaSuccess) e = cudaEventRecord(side->join, side->st);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, side->join, 0);
     }

@@ -54,19 +54,39 @@ flag_fp64_kernel(Problem p, Partials part, int row_tile0, int row_tiles) {
                                           (long long)blockIdx.y * row_tiles + row_tile, red, S);
 }
 
-// Band-independent frequencies: blockIdx.y covers NB occupied bands; a
-// block walks row tiles row_tile0 + blockIdx.x, + gridDim.x, ... below
-// row_tile0 + count.
+// Band-independent frequencies: blockIdx.y covers NB occupied bands and
+// blockIdx.z a frequency chunk, blockIdx.x one of `count` row tiles from
+// row_tile0.  With `next` set, a persistent grid instead: each block takes
+// (row tile, band group, chunk) items from the counter until none is left,
+// so blocks that share an SM take fewer; every item is computed and written
+// as in the one-tile grid, so the bits do not depend on the grid.
 template <int RG, int NWC, int NB, int THREADS, int SEM>
 __global__ void __launch_bounds__(THREADS)
-flag_fp64_multi_kernel(Problem p, Partials part, int row_tile0, int count, int row_tiles) {
+flag_fp64_multi_kernel(Problem p, Partials part, int row_tile0, int count, int row_tiles,
+                       int *next) {
     constexpr int K = NB * RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    for (int t = blockIdx.x; t < count; t += gridDim.x) {
-        flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + t, blockIdx.y * NB,
-                                                        blockIdx.z, row_tiles, red, S);
-        __syncthreads();  // the epilogue has read S before the next tile reduces into it
+    __shared__ int item;
+    if (!next) {
+        flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + blockIdx.x,
+                                                        blockIdx.y * NB, blockIdx.z, row_tiles,
+                                                        red, S);
+        return;
+    }
+    const int groups = (p.nv + NB - 1) / NB;
+    const long long items = (long long)count * groups * ((p.nw + NWC - 1) / NWC);
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(next, 1);
+        __syncthreads();
+        const long long it = item;
+        if (it >= items) break;
+        const int t = (int)(it % count);
+        const long long rest = it / count;
+        flag_fp64_multi_tile<RG, NWC, NB, THREADS, SEM>(p, part, row_tile0 + t,
+                                                        (int)(rest % groups) * NB,
+                                                        (int)(rest / groups), row_tiles, red, S);
+        __syncthreads();  // S read by the epilogue, `item` by every thread, before reuse
     }
 }
 
@@ -154,25 +174,29 @@ int flag_blocks_per_sm(int asked) {
 
 template <int RG, int NWC, int NB, int THREADS>
 cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles r, int row_tiles,
-                                int blocks_per_sm, cudaStream_t s) {
+                                int blocks_per_sm, int *next, cudaStream_t s) {
     const int count = r.end - r.begin;
     dim3 grid(count, ceil_div(p.nv, NB), ceil_div(p.nw, NWC));
-    const int per_sm = flag_blocks_per_sm(blocks_per_sm);
+    const int per_sm = next ? flag_blocks_per_sm(blocks_per_sm) : 0;
     if (per_sm > 0) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long cap = (long long)std::max(sms, 1) * per_sm / ((long long)grid.y * grid.z);
-        grid.x = (unsigned)std::max(1ll, std::min<long long>(count, cap));
+        const long long items = (long long)count * grid.y * grid.z;
+        grid = dim3((unsigned)std::max(1ll, std::min<long long>(items, (long long)std::max(sms, 1) * per_sm)));
+        const cudaError_t e = cudaMemsetAsync(next, 0, sizeof(int), s);
+        if (e != cudaSuccess) return e;
+    } else {
+        next = nullptr;
     }
     if (p.semantics == kSemKerSeq) {
         prefer_max_shared(flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemKerSeq>);
         flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemKerSeq><<<grid, THREADS, 0, s>>>(
-            p, part, r.begin, count, row_tiles);
+            p, part, r.begin, count, row_tiles, next);
     } else {
         prefer_max_shared(flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemComplexSeq>);
         flag_fp64_multi_kernel<RG, NWC, NB, THREADS, kSemComplexSeq><<<grid, THREADS, 0, s>>>(
-            p, part, r.begin, count, row_tiles);
+            p, part, r.begin, count, row_tiles, next);
     }
     count_launch();
     return cudaGetLastError();
@@ -180,13 +204,14 @@ cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles
 
 template <int RG, int NWC, int THREADS>
 cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, int blocks_per_sm,
-                          cudaStream_t s) {
+                          int *next, cudaStream_t s) {
     const int row_tiles = ceil_div(p.ng, RG);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
     if constexpr (NWC <= 4) {  // two bands of 8 frequencies would spill
         if (p.wx_stride == 0 && p.nv >= 2 && flag_multi_enabled())
-            return launch_flag_multi_t<RG, NWC, 2, THREADS>(p, part, r, row_tiles, blocks_per_sm, s);
+            return launch_flag_multi_t<RG, NWC, 2, THREADS>(p, part, r, row_tiles, blocks_per_sm,
+                                                            next, s);
     }
     dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
     if (p.semantics == kSemKerSeq) {
@@ -228,14 +253,14 @@ cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int b0, i
 }
 
 cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s, RowTiles rt,
-                             int blocks_per_sm) {
+                             int blocks_per_sm, int *next) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
     switch (nwc_for(p.nw)) {
-        case 1: return launch_flag_t<2, 1, 128>(p, part, rt, blocks_per_sm, s);
-        case 2: return launch_flag_t<2, 2, 128>(p, part, rt, blocks_per_sm, s);
-        case 3: return launch_flag_t<2, 3, 128>(p, part, rt, blocks_per_sm, s);
-        case 4: return launch_flag_t<2, 4, 128>(p, part, rt, blocks_per_sm, s);
-        default: return launch_flag_t<2, 8, 128>(p, part, rt, blocks_per_sm, s);
+        case 1: return launch_flag_t<2, 1, 128>(p, part, rt, blocks_per_sm, next, s);
+        case 2: return launch_flag_t<2, 2, 128>(p, part, rt, blocks_per_sm, next, s);
+        case 3: return launch_flag_t<2, 3, 128>(p, part, rt, blocks_per_sm, next, s);
+        case 4: return launch_flag_t<2, 4, 128>(p, part, rt, blocks_per_sm, next, s);
+        default: return launch_flag_t<2, 8, 128>(p, part, rt, blocks_per_sm, next, s);
     }
 }
 

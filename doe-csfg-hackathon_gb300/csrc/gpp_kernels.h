@@ -41,11 +41,13 @@ struct RowTiles {
 cudaError_t launch_noflag_fp64(const Problem &p, const Partials &part, int band_begin,
                                int band_end, cudaStream_t s, RowTiles rows = RowTiles());
 // Occupied bands [0, nvband): full ssxt_scht_solver branch logic in FP64.
-// blocks_per_sm > 0 (band-independent frequencies only): a persistent grid of
-// that many blocks per SM walking the row tiles, for a launch beside the
-// tensor-core GEMM (GPP_FLAG_BLOCKS_PER_SM overrides it).
+// blocks_per_sm > 0 with a device counter `next` (band-independent
+// frequencies only): a persistent grid of that many blocks per SM taking row
+// tiles from the counter (zeroed on `s` first), for a launch beside the
+// tensor-core GEMM (GPP_FLAG_BLOCKS_PER_SM overrides blocks_per_sm).
 cudaError_t launch_flag_fp64(const Problem &p, const Partials &part, cudaStream_t s,
-                             RowTiles rows = RowTiles(), int blocks_per_sm = 0);
+                             RowTiles rows = RowTiles(), int blocks_per_sm = 0,
+                             int *next = nullptr);
 // Static term (reduce_achstemp) over all bands: one partial per block.
 int achstemp_blocks(const Problem &p);
 cudaError_t launch_achstemp(const Problem &p, double2 *partials, int *err, cudaStream_t s);
