@@ -405,10 +405,14 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
         e = cudaStreamWaitEvent(side->st, side->fork, 0);
         part.ach_tile0 = 0;
         if (e == cudaSuccess)
-            // Beside the tensor-core GEMM, one persistent block per SM: the
-            // GEMM's MMAs make no progress while FP64 instructions are in
-            // flight on an SM, and a lighter FP64 load leaves them more time.
-            e = mixed ? launch_flag_mixed(p, part, w + o_split, side->st)
+            // FP64 beside the tensor-core GEMM: one persistent block per SM
+            // taking row tiles from a counter.  The GEMM's MMAs slow down under
+            // any co-resident load and stop while FP64 instructions are in
+            // flight on their SM, so a lighter load leaves them more time.  The
+            // float-float kernel keeps its grid (three blocks per SM carry its
+            // FP32 work; one was slower).
+            e = mixed ? launch_flag_mixed(p, part, w + o_split, side->st, RowTiles(), 0,
+                                          reinterpret_cast<int *>(w + o_next))
                       : launch_flag_fp64(p, part, side->st, RowTiles(), gemm && tensor ? 1 : 0,
                                          reinterpret_cast<int *>(w + o_next));
         if (e == cudaSuccess) e = cudaEventRecord(side->join, side->st);

@@ -165,13 +165,6 @@ bool flag_multi_enabled() {
     return !(v && v[0] == '0');
 }
 
-// Blocks per SM of the occupied-band pair kernel (0: one block per row
-// tile); GPP_FLAG_BLOCKS_PER_SM, read on every call, overrides the caller's.
-int flag_blocks_per_sm(int asked) {
-    const char *v = getenv("GPP_FLAG_BLOCKS_PER_SM");
-    return v ? atoi(v) : asked;
-}
-
 template <int RG, int NWC, int NB, int THREADS>
 cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles r, int row_tiles,
                                 int blocks_per_sm, int *next, cudaStream_t s) {
@@ -228,6 +221,11 @@ cudaError_t launch_flag_t(const Problem &p, const Partials &part, RowTiles rt, i
 }
 
 }  // namespace
+
+int flag_blocks_per_sm(int asked) {
+    const char *v = getenv("GPP_FLAG_BLOCKS_PER_SM");
+    return v ? atoi(v) : asked;
+}
 
 // Frequencies per block: a whole small frequency grid stays in registers; a
 // large grid (e.g. 32 frequencies) is split into chunks of 8.

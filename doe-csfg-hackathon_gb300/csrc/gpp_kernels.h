@@ -83,8 +83,13 @@ bool mixed_variant_valid(int variant, int nw);
 cudaError_t launch_mixed_noflag(const Problem &p, const Partials &part, void *split_ws,
                                 int band_begin, int band_end, cudaStream_t s, int variant,
                                 RowTiles rows = RowTiles());
+// blocks_per_sm and next as for launch_flag_fp64.
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
-                              cudaStream_t s, RowTiles rows = RowTiles());
+                              cudaStream_t s, RowTiles rows = RowTiles(), int blocks_per_sm = 0,
+                              int *next = nullptr);
+// Blocks per SM of a persistent occupied-band grid (0: one block per tile);
+// GPP_FLAG_BLOCKS_PER_SM, read on every call, overrides the caller's choice.
+int flag_blocks_per_sm(int asked);
 // One block that waits on an mbarrier nothing arrives at and records the
 // bounded-wait timeout in *err (exercises the failure path without a fault).
 cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t s);

@@ -288,30 +288,64 @@ cudaError_t launch_split(const Problem &p, void *split_ws, int b0, int b1, cudaS
 // compiler's 222-register choice by 15% (4 blocks spilled and lost).
 template <int RG, int NWC, int THREADS, int SEM>
 __global__ void __launch_bounds__(THREADS, NWC <= 4 ? 3 : 2)
-flag_mixed_kernel(Problem p, Partials part, SplitPlanes s, int row_tile0, int row_tiles) {
+flag_mixed_kernel(Problem p, Partials part, SplitPlanes s, int row_tile0, int count,
+                  int row_tiles, int *next) {
     constexpr int K = RG * NWC * 4;
     __shared__ double red[(THREADS / 32) * K];
     __shared__ double S[K];
-    const int row_tile = row_tile0 + blockIdx.x;
-    flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, row_tile, blockIdx.y, blockIdx.z,
-                                           (long long)blockIdx.y * row_tiles + row_tile, red, S);
+    __shared__ int item;
+    if (!next) {
+        const int row_tile = row_tile0 + blockIdx.x;
+        flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, row_tile, blockIdx.y, blockIdx.z,
+                                               (long long)blockIdx.y * row_tiles + row_tile, red,
+                                               S);
+        return;
+    }
+    // Persistent grid beside the tensor-core GEMM: (row tile, band, chunk)
+    // items from the counter, each computed and written as in the grid above.
+    const long long items = (long long)count * p.nv * ((p.nw + NWC - 1) / NWC);
+    for (;;) {
+        if (threadIdx.x == 0) item = atomicAdd(next, 1);
+        __syncthreads();
+        const long long it = item;
+        if (it >= items) break;
+        const int row_tile = row_tile0 + (int)(it % count);
+        const long long rest = it / count;
+        const int band = (int)(rest % p.nv);
+        flag_mixed_tile<RG, NWC, THREADS, SEM>(p, part, s, row_tile, band, (int)(rest / p.nv),
+                                               (long long)band * row_tiles + row_tile, red, S);
+        __syncthreads();  // S read by the epilogue, `item` by every thread, before reuse
+    }
 }
 
 template <int NWC>
 cudaError_t launch_flag_mixed_t(const Problem &p, const Partials &part, const SplitPlanes &s,
-                                RowTiles rt, cudaStream_t st) {
+                                RowTiles rt, int blocks_per_sm, int *next, cudaStream_t st) {
     const int row_tiles = ceil_div(p.ng, 2);
     const RowTiles r = rt.clip(row_tiles);
     if (r.end <= r.begin) return cudaSuccess;
-    dim3 grid(r.end - r.begin, p.nv, ceil_div(p.nw, NWC));
+    const int count = r.end - r.begin;
+    dim3 grid(count, p.nv, ceil_div(p.nw, NWC));
+    const int per_sm = next ? flag_blocks_per_sm(blocks_per_sm) : 0;
+    if (per_sm > 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const long long items = (long long)count * grid.y * grid.z;
+        grid = dim3((unsigned)std::max(1ll, std::min<long long>(items, (long long)std::max(sms, 1) * per_sm)));
+        const cudaError_t e = cudaMemsetAsync(next, 0, sizeof(int), st);
+        if (e != cudaSuccess) return e;
+    } else {
+        next = nullptr;
+    }
     if (p.semantics == kSemKerSeq) {
         prefer_max_shared(flag_mixed_kernel<2, NWC, 128, kSemKerSeq>);
         flag_mixed_kernel<2, NWC, 128, kSemKerSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
-                                                                        row_tiles);
+                                                                        count, row_tiles, next);
     } else {
         prefer_max_shared(flag_mixed_kernel<2, NWC, 128, kSemComplexSeq>);
-        flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(p, part, s, r.begin,
-                                                                            row_tiles);
+        flag_mixed_kernel<2, NWC, 128, kSemComplexSeq><<<grid, 128, 0, st>>>(
+            p, part, s, r.begin, count, row_tiles, next);
     }
     count_launch();
     return cudaGetLastError();
@@ -344,15 +378,15 @@ cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t st) {
 }
 
 cudaError_t launch_flag_mixed(const Problem &p, const Partials &part, void *split_ws,
-                              cudaStream_t st, RowTiles rt) {
+                              cudaStream_t st, RowTiles rt, int blocks_per_sm, int *next) {
     if (p.nv <= 0 || p.ng == 0) return cudaSuccess;
     const SplitPlanes s = planes(p, split_ws);
     switch (nwc_for(p.nw)) {
-        case 1: return launch_flag_mixed_t<1>(p, part, s, rt, st);
-        case 2: return launch_flag_mixed_t<2>(p, part, s, rt, st);
-        case 3: return launch_flag_mixed_t<3>(p, part, s, rt, st);
-        case 4: return launch_flag_mixed_t<4>(p, part, s, rt, st);
-        default: return launch_flag_mixed_t<8>(p, part, s, rt, st);
+        case 1: return launch_flag_mixed_t<1>(p, part, s, rt, blocks_per_sm, next, st);
+        case 2: return launch_flag_mixed_t<2>(p, part, s, rt, blocks_per_sm, next, st);
+        case 3: return launch_flag_mixed_t<3>(p, part, s, rt, blocks_per_sm, next, st);
+        case 4: return launch_flag_mixed_t<4>(p, part, s, rt, blocks_per_sm, next, st);
+        default: return launch_flag_mixed_t<8>(p, part, s, rt, blocks_per_sm, next, st);
     }
 }
 
