@@ -10,7 +10,7 @@
 //
 //  * every real operand value x of row (or column) l and k chunk c is
 //    written as x = 2^e sum_{i=1..S} s_i 2^(-7 i), e the chunk's common
-//    exponent (max |x| < 2^e), s_1 in [-128, 128] and s_i in [-64, 64]:
+//    exponent (max |x| < 2^e), s_1 in [-128, 128] and s_i in [-64, 63]:
 //    integers, held exactly in bf16 (8 significant bits).  S = 8 slices keep
 //    56 bits of the chunk's largest value;
 //  * a product of two slices summed over a chunk of at most 512 k values is
@@ -19,9 +19,9 @@
 //    with operands up to 128, with mma.sync and with tcgen05.mma);
 //  * pairs (i, j) with the same i + j = d share the scale 2^(-7 d); those
 //    whose worst-case sums still fit in 2^24 are summed in one accumulator
-//    (10 groups for the 36 pairs with i + j <= 9), each group's exact
-//    integer sum is stored, and a combining pass scales the group sums and
-//    adds them in float-float;
+//    (10 groups for the 36 pairs with i + j <= 9), the groups' exact
+//    integer sums are stored two to an int32, and a combining pass scales
+//    them and adds them in float-float;
 //  * pairs with i + j > 9 fall below 2^-56 of the largest products and are
 //    left out, as are bits past the 8th slice.
 //
@@ -413,14 +413,16 @@ __device__ __forceinline__ TcStep tc_decode(int t, int KS, int nch_here) {
 // The tensor-core products on tcgen05: block (bx, by, z) computes rows
 // [128 (mt0 + bx), +128) of X against rows [256 by, +256) of Y over split
 // z's chunks, its group sums stored at slab row 128 bx + ... (slab of Ms
-// rows), packed in pairs (kSlotD).  Warp 0 (one thread) streams each step's two operand blocks into a
+// rows), packed in pairs (kSlotD).  Warp 0 (one thread) streams each step's
+// two operand blocks into a
 // four-stage shared-memory ring with 1-D bulk copies completing on full[s];
 // warp 1 (one thread) issues four K = 16 tcgen05.mma per step into one of two
 // TMEM accumulators (128 lanes x 256 FP32 columns each) and commits to
 // empty[s], and at a group's end to accfull[a]; warps 2-5 read a finished
 // accumulator (each warp its 32 TMEM lanes, 32 columns per tcgen05.ld),
-// store the group's exact sums at fold[((((z 3 + g) cps + cl) kGroups +
-// group) Mp + m) Np + n] and release it on accempty[a].  Every wait is
+// store the group's exact sums as int32 at fold[((((z 3 + g) cps + cl)
+// kSlots + group / 2) Ms + m) Np + n] (an odd group packed with the even one
+// stored there before it) and release it on accempty[a].  Every wait is
 // bounded; a block that gives up records kErrPipelineTimeout, lets its
 // copies and MMAs finish and frees its TMEM.
 __global__ void __launch_bounds__(kTcThreads, 1)
