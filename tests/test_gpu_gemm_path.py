@@ -203,3 +203,41 @@ def test_occupied_band_pairs_give_the_per_band_bits(shape, semantics, monkeypatc
         a = getattr(pair, key).cpu().numpy()
         assert np.array_equal(a, getattr(single, key).cpu().numpy()), key
         assert np.array_equal(a, getattr(replicated, key).cpu().numpy()), key
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("shape,semantics", [
+    (W.Shape(48, 2, 1500, 301, 3, near_pole=0.05), "complex_seq"),
+    (W.Shape(40, 5, 900, 37, 4), "kerseq"),
+    (W.Shape(36, 3, 700, 19, 8, dw=0.25), "complex_seq"),
+])
+def test_occupied_band_grid_beside_the_tensor_gemm_keeps_the_bits(precision, shape, semantics,
+                                                                   monkeypatch):
+    """Beside the tensor-core GEMM the occupied-band kernel may run as a
+    persistent grid taking (row tile, band group, chunk) items from a work
+    counter (the FP64 default), one block per row tile (the float-float
+    default) or before the GEMM on the same stream (GPP_OVERLAP_TENSOR_GEMM=0);
+    every item is computed and written the same way and the partials are
+    reduced in one fixed order, so every choice gives the same bits."""
+    from gppsigma import ops
+    d = ops.DeviceInputs.from_host(band_independent(shape, 31))
+    lib = capi.load()
+
+    def run():
+        capi.check(lib.gpp_set_gemm_path(1), "gemm path")
+        try:
+            r = ops.sigma(d, precision, semantics, acht_n1=True)
+            ops.wait()
+        finally:
+            capi.check(lib.gpp_set_gemm_path(-1), "gemm path")
+        return {k: getattr(r, k).cpu().numpy() for k in ("achtemp", "asxtemp", "acht_n1_loc")}
+
+    base = run()
+    for env in ({"GPP_FLAG_BLOCKS_PER_SM": "0"}, {"GPP_FLAG_BLOCKS_PER_SM": "1"},
+                {"GPP_FLAG_BLOCKS_PER_SM": "2"}, {"GPP_OVERLAP_TENSOR_GEMM": "0"}):
+        with monkeypatch.context() as m:
+            for k, v in env.items():
+                m.setenv(k, v)
+            got = run()
+        for key, want in base.items():
+            assert np.array_equal(got[key], want), (env, key)
