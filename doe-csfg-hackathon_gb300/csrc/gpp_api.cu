@@ -376,7 +376,7 @@ gpp_status run_sigma(const Problem &p, int b0, int b1, int precision, const OutS
                 if (st == GPP_OK)
                     st = mixed_gemm_rows(p, part, w + o_split, w + o_gemm, nb0, nb1, s, rt);
                 if (st == GPP_OK && k == pc.n - 1)
-                    st = tensor ? gemm_per_band(p, part, w + o_gemm64, nb0, nb1, s)
+                    st = tensor ? gemm_per_band(p, part, w + o_gemm64, nb0, nb1, s, w + o_split)
                                 : mixed_gemm_per_band(p, part, w + o_split, w + o_gemm, nb0, nb1, s);
                 if (st != GPP_OK) {
                     cudaFreeAsync(ws, s);

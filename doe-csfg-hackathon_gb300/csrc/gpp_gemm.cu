@@ -36,6 +36,7 @@
 #include <cstdio>
 
 #include "gpp_gemm.h"
+#include "gpp_gemm_mixed.h"
 #include "gpp_ozaki.h"
 
 namespace gpp {
@@ -425,14 +426,20 @@ gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, i
 }
 
 gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                         cudaStream_t s) {
+                         cudaStream_t s, void *split_ws) {
     const int K = b1 - b0;
     if (K <= 0 || p.ng <= 0 || !part.n1) return GPP_OK;
     const GemmBuffers b = carve(p, ws, K, true);
-    gemm_m2_kernel<<<grid_for((long long)p.ng * p.nc), kThreads, 0, s>>>(p, 0, p.ng, b.M2);
-    count_launch();
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
+    cudaError_t e = cudaSuccess;
+    if (split_ws) {
+        const gpp_status st = mixed_m2_fp64(p, split_ws, b0, b.M2, s);
+        if (st != GPP_OK) return st;
+    } else {
+        gemm_m2_kernel<<<grid_for((long long)p.ng * p.nc), kThreads, 0, s>>>(p, 0, p.ng, b.M2);
+        count_launch();
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "gemm_m2_kernel");
+    }
     // H (K x ng) = aqsn M_2^T: X(k', ig) = aqsn[b0 + k'][ig], Y(r, ig) = M_2[r][ig],
     // the ncouls sum split up to h_splits() ways.
     int splits;

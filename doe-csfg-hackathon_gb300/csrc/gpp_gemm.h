@@ -30,8 +30,10 @@ gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b
                          cudaStream_t s);
 gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, int b1,
                      cudaStream_t s, RowTiles rows = RowTiles());
+// split_ws: the mixed path's split planes; M_2 is then formed in float-float
+// from them (mixed_m2_fp64) instead of in FP64.
 gpp_status gemm_per_band(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                         cudaStream_t s);
+                         cudaStream_t s, void *split_ws = nullptr);
 
 // G (ng x nc, FP64) inside a workspace of gemm_bytes(p, bands, want_n1),
 // written by gemm_band_sum.

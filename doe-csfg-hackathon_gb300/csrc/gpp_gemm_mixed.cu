@@ -19,6 +19,7 @@
 // acht_n1_loc is a second product of the same form, H = aqsn M_2^T, with
 // its long sum over columns split into chunks that are added in order.
 #include "gpp_gemm_mixed.h"
+#include "gpp_ozaki_split.cuh"
 #include "gpp_tiles_mixed.cuh"
 
 namespace gpp {
@@ -308,6 +309,26 @@ static __device__ __noinline__ TermPair mg_pole_m2(const Problem &p, df2 d, floa
     return t;
 }
 
+// M_2 of row pair j, column ig (both rows as the lanes).
+__device__ __forceinline__ TermPair m2_pair(const Problem &p, const SplitPlanes &s, df wx,
+                                            float thr, size_t j, size_t ig) {
+    const size_t nc = (size_t)p.nc;
+    const float4 *rp = s.rows + j * 4 * nc;
+    const float4 vr = __ldg(rp + ig), vi = __ldg(rp + nc + ig);
+    const float4 vqr = __ldg(rp + 2 * nc + ig), vqi = __ldg(rp + 3 * nc + ig);
+    const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)}, wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
+    const df2 qr = {f2(vqr.x, vqr.y), f2(vqr.z, vqr.w)};
+    const df2 qi = {f2(vqi.x, vqi.y), f2(vqi.z, vqi.w)};
+    const df2 wr = df2_norm(df2_sub(df2_bcast(wx), wtr));
+    const df2 d = df2_add(df2_sqr(wr), df2_mul(wti, wti));
+    const df2 r = df2_rcp(d);
+    TermPair t;
+    t.re = df2_mul(df2_sub(df2_mul(qr, wr), df2_mul(qi, wti)), r);
+    t.im = df2_mul(df2_add(df2_mul(qi, wr), df2_mul(qr, wti)), r);
+    if (!(d.h.x >= thr) || !(d.h.y >= thr)) t = mg_pole_m2(p, d, thr, (int)(2 * j), (int)ig, t);
+    return t;
+}
+
 __global__ void __launch_bounds__(kThreads) mg_m2_kernel(Problem p, SplitPlanes s, int wx_band,
                                                          float4 *M2) {
     const int pairs = (p.ng + 1) / 2;
@@ -319,21 +340,32 @@ __global__ void __launch_bounds__(kThreads) mg_m2_kernel(Problem p, SplitPlanes 
     for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
          i += (size_t)gridDim.x * kThreads) {
         const size_t j = i / nc, ig = i % nc;
-        const float4 *rp = s.rows + j * 4 * nc;
-        const float4 vr = __ldg(rp + ig), vi = __ldg(rp + nc + ig);
-        const float4 vqr = __ldg(rp + 2 * nc + ig), vqi = __ldg(rp + 3 * nc + ig);
-        const df2 wtr = {f2(vr.x, vr.y), f2(vr.z, vr.w)}, wti = {f2(vi.x, vi.y), f2(vi.z, vi.w)};
-        const df2 qr = {f2(vqr.x, vqr.y), f2(vqr.z, vqr.w)};
-        const df2 qi = {f2(vqi.x, vqi.y), f2(vqi.z, vqi.w)};
-        const df2 wr = df2_norm(df2_sub(df2_bcast(wx), wtr));
-        const df2 d = df2_add(df2_sqr(wr), df2_mul(wti, wti));
-        const df2 r = df2_rcp(d);
-        TermPair t;
-        t.re = df2_mul(df2_sub(df2_mul(qr, wr), df2_mul(qi, wti)), r);
-        t.im = df2_mul(df2_add(df2_mul(qi, wr), df2_mul(qr, wti)), r);
-        if (!(d.h.x >= thr) || !(d.h.y >= thr)) t = mg_pole_m2(p, d, thr, (int)(2 * j), (int)ig, t);
+        const TermPair t = m2_pair(p, s, wx, thr, j, ig);
         M2[j * 2 * nc + ig] = make_float4(t.re.h.x, t.re.h.y, t.re.l.x, t.re.l.y);
         M2[j * 2 * nc + nc + ig] = make_float4(t.im.h.x, t.im.h.y, t.im.l.x, t.im.l.y);
+    }
+}
+
+// The same M_2 as FP64 rows M[r][ig] (ng x nc), for the tensor-core
+// per-band GEMM of the mixed path: the float-float lanes assembled into
+// doubles on the integer pipes (no FP64 instruction but at the pole).
+__global__ void __launch_bounds__(kThreads) mg_m2_fp64_kernel(Problem p, SplitPlanes s,
+                                                              int wx_band, double2 *M) {
+    const int pairs = (p.ng + 1) / 2;
+    const size_t nc = (size_t)p.nc;
+    const float2 x = s.wx[(size_t)wx_band * p.nw + 2];
+    const df wx = {x.x, x.y};
+    const float thr = 1e-6f * x.x * x.x;
+    const size_t n = (size_t)pairs * nc;
+    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * kThreads) {
+        const size_t j = i / nc, ig = i % nc;
+        const TermPair t = m2_pair(p, s, wx, thr, j, ig);
+        M[2 * j * nc + ig] = make_double2(oz_df_to_double(t.re.h.x, t.re.l.x),
+                                          oz_df_to_double(t.im.h.x, t.im.l.x));
+        if (2 * j + 1 < (size_t)p.ng)
+            M[(2 * j + 1) * nc + ig] = make_double2(oz_df_to_double(t.re.h.y, t.re.l.y),
+                                                    oz_df_to_double(t.im.h.y, t.im.l.y));
     }
 }
 
@@ -503,6 +535,18 @@ gpp_status mixed_gemm_rows(const Problem &p, const Partials &part, void *split_w
         default: e = launch_freq_t<8>(p, part, s, b0, G, rt, st); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "mg_freq_kernel");
+    return GPP_OK;
+}
+
+gpp_status mixed_m2_fp64(const Problem &p, void *split_ws, int wx_band, double2 *M,
+                         cudaStream_t st) {
+    const int pairs = row_pairs(p);
+    if (pairs <= 0) return GPP_OK;
+    const SplitPlanes s = split_planes_at(p, split_ws);
+    mg_m2_fp64_kernel<<<grid_for((long long)pairs * p.nc), kThreads, 0, st>>>(p, s, wx_band, M);
+    count_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "mg_m2_fp64_kernel");
     return GPP_OK;
 }
 

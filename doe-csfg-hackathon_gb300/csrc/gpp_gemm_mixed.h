@@ -37,4 +37,11 @@ gpp_status mixed_gemm_per_band(const Problem &p, const Partials &part, void *spl
 gpp_status mixed_gemm_planes_from(const Problem &p, void *ws, int b0, int b1, const double2 *G,
                                   cudaStream_t st);
 
+// M_2 = Q conj(wdiff) / |wdiff|^2 at iw = 2 (the per-band product's right
+// operand) as FP64 rows M[r][ig], computed in float-float from the split row
+// planes (FP64 within 1e-3 |wx| of the pole) with wx of band wx_band: the
+// mixed path's operand of the tensor-core per-band GEMM.
+gpp_status mixed_m2_fp64(const Problem &p, void *split_ws, int wx_band, double2 *M,
+                         cudaStream_t st);
+
 }  // namespace gpp

@@ -631,16 +631,6 @@ __device__ __forceinline__ void split_packed(int v, float &hi, float &lo) {
     hi = __fmul_rn(__fsub_rn(__int_as_float(0x4B400000 + (v >> 16)), 12582912.0f), 65536.0f);
 }
 
-// The double of a float-float pair: renormalised by TwoSum (exact), then
-// assembled from the bits; FP64 only for a subnormal or non-finite head.
-__device__ __forceinline__ double df_to_double(float h, float l) {
-    const float s = __fadd_rn(h, l);
-    const float bb = __fsub_rn(s, h);
-    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(l, bb));
-    bool ok;
-    const double d = oz_pair_to_double(s, e, &ok);
-    return ok ? d : (double)s + (double)e;
-}
 
 // d 2^e: the exponent field moved when d and the result are normal doubles
 // (exact, as scalbn is), scalbn otherwise (off the common path).
@@ -738,7 +728,8 @@ __global__ void __launch_bounds__(256) oz_combine_kernel(const int *fold, const 
             df_add(PH[0][j], PL[0][j], -PH[1][j], -PL[1][j], rh, rl);
             df_add(PH[0][j], PL[0][j], PH[1][j], PL[1][j], bh, bl);
             df_add(PH[2][j], PL[2][j], -bh, -bl, ih, il);
-            double2 o = make_double2(scale2(df_to_double(rh, rl), e), scale2(df_to_double(ih, il), e));
+            double2 o = make_double2(scale2(oz_df_to_double(rh, rl), e),
+                                     scale2(oz_df_to_double(ih, il), e));
             if (exm >= kNonFiniteExp || eyn[j] >= kNonFiniteExp)
                 o = make_double2(__longlong_as_double(0x7FF8000000000000ll),
                                  __longlong_as_double(0x7FF8000000000000ll));

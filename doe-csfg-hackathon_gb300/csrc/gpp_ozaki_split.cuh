@@ -168,4 +168,21 @@ __host__ __device__ __forceinline__ double oz_pair_to_double(float h, float l, b
                      ((unsigned long long)D & 0xFFFFFFFFFFFFFull));
 }
 
+// The double of any float-float pair h + l: renormalised by TwoSum (exact),
+// then assembled from the bits; FP64 only for a subnormal or non-finite head.
+__host__ __device__ __forceinline__ double oz_df_to_double(float h, float l) {
+#ifdef __CUDA_ARCH__
+    const float s = __fadd_rn(h, l);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(l, bb));
+#else
+    const float s = h + l;
+    const float bb = s - h;
+    const float e = (h - (s - bb)) + (l - bb);
+#endif
+    bool ok;
+    const double d = oz_pair_to_double(s, e, &ok);
+    return ok ? d : (double)s + (double)e;
+}
+
 }  // namespace gpp
