@@ -46,14 +46,18 @@ __host__ __device__ __forceinline__ long long oz_fixed_point(double x, int e) {
 // The balanced base-128 digits of oz_fixed_point(x, e), most significant
 // first: d[1..S-1] in [-64, 63], d[0] the rest (|d[0]| <= 128).  Integers of
 // at most 8 significant bits, so exact in bf16.
-// The balanced base-128 digits of a fixed-point value N, |N| <= 2^56 + 1.
+// The balanced base-128 digits of a fixed-point value N, |N| <= 2^56 + 1:
+// d_2..d_8 in [-64, 63] and d_1 the rest, N = sum_i d_i 128^(8 - i).  With
+// B = 64 (1 + 128 + ... + 128^6), M = N + B has the plain base-128 digits
+// d_i + 64 below its top (floor) digit d_1, so every digit is a shift and a
+// mask of M, without the carry chain of peeling them off one by one (the
+// representation is unique, so the digits are the same).
+constexpr long long kOzBalance = 64 * (((1ll << 49) - 1) / 127);
 __host__ __device__ __forceinline__ void oz_digits(long long N, int (&d)[kOzSlices]) {
+    const long long M = N + kOzBalance;
 #pragma unroll
-    for (int i = kOzSlices - 1; i >= 1; --i) {
-        d[i] = (int)((N + 64) & 127) - 64;
-        N = (N - d[i]) >> 7;
-    }
-    d[0] = (int)N;
+    for (int i = 1; i < kOzSlices; ++i) d[i] = (int)((M >> (7 * (kOzSlices - 1 - i))) & 127) - 64;
+    d[0] = (int)(M >> (7 * (kOzSlices - 1)));
 }
 
 __host__ __device__ __forceinline__ void oz_slices(double x, int e, int (&d)[kOzSlices]) {
