@@ -386,7 +386,7 @@ const double2 *gemm_g(const Problem &p, void *ws, int bands, bool want_n1) {
 }
 
 gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                         cudaStream_t s) {
+                         cudaStream_t s, cudaEvent_t after_slices) {
     const int K = b1 - b0;
     if (K <= 0 || p.ng <= 0) return GPP_OK;
     const GemmBuffers b = carve(p, ws, K, part.n1 != nullptr);
@@ -398,12 +398,13 @@ gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b
     // G (ng x nc) = C^T aqsn: X(r, k) = C[k][r], Y(ig, k) = aqsn[b0 + k][ig].
     if (fp64_gemm_on_tensor_cores()) {
         const OzOperand X{b.C, p.ng, false, p.ng}, Y{p.aqsn + (size_t)b0 * p.nc, p.nc, false, p.nc};
-        e = ozaki_zgemm(X, Y, p.ng, p.nc, K, 1, b.G, p.nc, 0, b.oz, part.err, s);
+        e = ozaki_zgemm(X, Y, p.ng, p.nc, K, 1, b.G, p.nc, 0, b.oz, part.err, s, after_slices);
         if (e != cudaSuccess) return cuda_fail(e, "ozaki_zgemm (band sum)");
         return GPP_OK;
     }
     e = launch_zgemm3m<false, false>(b.C, p.ng, p.aqsn + (size_t)b0 * p.nc, p.nc, b.G, p.nc, 0,
                                      p.ng, p.nc, K, 1, s);
+    if (e == cudaSuccess && after_slices) e = cudaEventRecord(after_slices, s);
     if (e != cudaSuccess) return cuda_fail(e, "zgemm3m_kernel (band sum)");
     return GPP_OK;
 }

@@ -26,8 +26,10 @@ size_t gemm_bytes(const Problem &p, int bands, bool want_n1);
 //  3. gemm_per_band: when part.n1 is set (nw >= 3), the per-band partials
 //     of acht_n1_loc -- needs every row.
 // `ws` holds gemm_bytes(p, b1 - b0, part.n1 != nullptr).
+// after_slices: recorded on s once the tensor-core GEMM's slicing passes are
+// queued (at the end of the call on the FP64-pipe path).
 gpp_status gemm_band_sum(const Problem &p, const Partials &part, void *ws, int b0, int b1,
-                         cudaStream_t s);
+                         cudaStream_t s, cudaEvent_t after_slices = nullptr);
 gpp_status gemm_rows(const Problem &p, const Partials &part, void *ws, int b0, int b1,
                      cudaStream_t s, RowTiles rows = RowTiles());
 // split_ws: the mixed path's split planes; M_2 is then formed in float-float

@@ -762,7 +762,7 @@ int ozaki_splits(int K, int splits) { return geometry(1, 1, K, splits).splits; }
 
 cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, int K, int splits,
                         double2 *Out, long long out_ld, long long split_stride, void *ws, int *err,
-                        cudaStream_t s) {
+                        cudaStream_t s, cudaEvent_t after_slices) {
     if (M <= 0 || N <= 0) return cudaSuccess;
     const Geometry g = geometry(M, N, K, splits);
     if (g.Mp / kTM > 65535 || g.Np / kTN > 65535 || g.splits > 65535)
@@ -779,9 +779,11 @@ cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, in
                                                                         kTM, b.ex, b.sx);
     oz_split_kernel<<<grid_for((long long)g.Np * g.Kp / 8), 256, 0, s>>>(Y, K, g.Kc, g.Kp, g.Np,
                                                                         kTN, b.ey, b.sy);
+    cudaError_t e = after_slices ? cudaEventRecord(after_slices, s) : cudaSuccess;
+    if (e != cudaSuccess) return e;
     static std::atomic<bool> configured[256] = {};
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (!configured[dev & 255].load(std::memory_order_acquire)) {
         e = cudaFuncSetAttribute(oz_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

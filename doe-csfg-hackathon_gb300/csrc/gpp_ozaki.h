@@ -30,8 +30,10 @@ int ozaki_splits(int K, int splits);
 // added in split order by the caller).  Accuracy is that of an FP64 3M-form
 // GEMM; the products run on the tensor cores (tcgen05).  A block whose
 // bounded pipeline wait ran out sets kErrPipelineTimeout in *err.
+// after_slices, when given, is recorded on s once the slicing passes are
+// queued (before the tensor-core passes).
 cudaError_t ozaki_zgemm(const OzOperand &X, const OzOperand &Y, int M, int N, int K, int splits,
                         double2 *Out, long long out_ld, long long split_stride, void *ws, int *err,
-                        cudaStream_t s);
+                        cudaStream_t s, cudaEvent_t after_slices = nullptr);
 
 }  // namespace gpp
