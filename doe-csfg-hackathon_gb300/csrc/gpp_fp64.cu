@@ -170,12 +170,13 @@ cudaError_t launch_flag_multi_t(const Problem &p, const Partials &part, RowTiles
                                 int blocks_per_sm, int *next, cudaStream_t s) {
     const int count = r.end - r.begin;
     dim3 grid(count, ceil_div(p.nv, NB), ceil_div(p.nw, NWC));
-    const int per_sm = next ? flag_blocks_per_sm(blocks_per_sm) : 0;
+    // The counter is a 32-bit int: past 2^30 items the one-tile grid instead.
+    const long long items = (long long)count * grid.y * grid.z;
+    const int per_sm = next && items < (1ll << 30) ? flag_blocks_per_sm(blocks_per_sm) : 0;
     if (per_sm > 0) {
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const long long items = (long long)count * grid.y * grid.z;
         grid = dim3((unsigned)std::max(1ll, std::min<long long>(items, (long long)std::max(sms, 1) * per_sm)));
         const cudaError_t e = cudaMemsetAsync(next, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
