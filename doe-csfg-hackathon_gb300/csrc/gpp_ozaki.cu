@@ -633,12 +633,14 @@ __device__ __forceinline__ void split_packed(int v, float &hi, float &lo) {
 
 
 // d 2^e: the exponent field moved when d and the result are normal doubles
-// (exact, as scalbn is), scalbn otherwise (off the common path).
+// (exact, as scalbn is), a zero returned as it is, scalbn otherwise (off the
+// common path).
 __device__ __forceinline__ double scale2(double d, int e) {
     const int hi = __double2hiint(d);
     const int ed = (hi >> 20) & 0x7FF;
     if (ed != 0 && ed != 0x7FF && ed + e >= 1 && ed + e <= 2046)
         return __hiloint2double(hi + (e << 20), __double2loint(d));
+    if (((hi & 0x7FFFFFFF) | __double2loint(d)) == 0) return d;  // a zero stays itself
     return scalbn(d, e);
 }
 
