@@ -5,7 +5,8 @@ sizes, several k chunks and k splits, a wide dynamic range along k, and
 operands whose slices take the extreme values (s_1 = 128, s_2..s_8 = -64:
 the group sums reach 2^23, where FP32 accumulation must still be exact), and
 compares with sums in long double; an Inf or NaN input turns its row's or
-column's results into NaN and leaves the others alone.  The bound is 1e-13 of the largest
+column's results into NaN and leaves the others alone; small integer operands
+give the exact integer result, bit for bit.  The bound is 1e-13 of the largest
 result, normwise (an FP64 3M-form GEMM is ~1e-15 to 1e-14 here); the
 device fault word must stay clear.
 """
@@ -158,8 +159,61 @@ static int run_nonfinite() {
     return bad ? 1 : 0;
 }
 
+// Integer operands, |re|, |im| <= 2^(bits - 1): every slice product, group
+// sum, packed pair and float-float sum is exact, and so is the 3M
+// combination of integers, so the GEMM must equal the exact integer result
+// bit for bit.
+static int run_exact(int M, int N, int K, bool kfast, int bits) {
+    std::vector<double2> X((size_t)M * K), Y((size_t)N * K);
+    const long long span = 1ll << bits;
+    auto rnd = [&]() { return (double)((long long)(uni() * span) - span / 2); };
+    for (auto &v : X) v = make_double2(rnd(), rnd());
+    for (auto &v : Y) v = make_double2(rnd(), rnd());
+    std::vector<double2> Xd(X.size()), Yd(Y.size());
+    for (int m = 0; m < M; ++m)
+        for (int k = 0; k < K; ++k)
+            Xd[kfast ? (size_t)m * K + k : (size_t)k * M + m] = X[(size_t)m * K + k];
+    for (int n = 0; n < N; ++n)
+        for (int k = 0; k < K; ++k)
+            Yd[kfast ? (size_t)n * K + k : (size_t)k * N + n] = Y[(size_t)n * K + k];
+    double2 *dX, *dY, *dO;
+    void *ws;
+    int *derr;
+    if (cudaMalloc(&dX, X.size() * 16) || cudaMalloc(&dY, Y.size() * 16) ||
+        cudaMalloc(&dO, (size_t)M * N * 16) || cudaMalloc(&ws, gpp::ozaki_bytes(M, N, K, 1)) ||
+        cudaMalloc(&derr, 4))
+        return 3;
+    cudaMemcpy(dX, Xd.data(), X.size() * 16, cudaMemcpyHostToDevice);
+    cudaMemcpy(dY, Yd.data(), Y.size() * 16, cudaMemcpyHostToDevice);
+    cudaMemset(derr, 0, 4);
+    const gpp::OzOperand ox{dX, kfast ? K : M, kfast, M}, oy{dY, kfast ? K : N, kfast, N};
+    if (gpp::ozaki_zgemm(ox, oy, M, N, K, 1, dO, N, 0, ws, derr, 0) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess)
+        return 4;
+    std::vector<double2> O((size_t)M * N);
+    cudaMemcpy(O.data(), dO, O.size() * 16, cudaMemcpyDeviceToHost);
+    long long wrong = 0;
+    for (int m = 0; m < M; ++m)
+        for (int n = 0; n < N; ++n) {
+            long long re = 0, im = 0;
+            for (int k = 0; k < K; ++k) {
+                const double2 a = X[(size_t)m * K + k], b = Y[(size_t)n * K + k];
+                re += (long long)a.x * (long long)b.x - (long long)a.y * (long long)b.y;
+                im += (long long)a.x * (long long)b.y + (long long)a.y * (long long)b.x;
+            }
+            const double2 o = O[(size_t)m * N + n];
+            if (o.x != (double)re || o.y != (double)im) ++wrong;
+        }
+    printf("exact: M %d N %d K %d kfast %d, %d-bit integers: %lld results differ\n", M, N, K,
+           (int)kfast, bits, wrong);
+    cudaFree(dX); cudaFree(dY); cudaFree(dO); cudaFree(ws); cudaFree(derr);
+    return wrong ? 1 : 0;
+}
+
 int main() {
     int bad = 0;
+    bad |= run_exact(70, 300, 500, false, 15);
+    bad |= run_exact(45, 260, 1700, true, 13);
     bad |= run_nonfinite();
     bad |= run(37, 300, 510, 1, false, 0, false);
     bad |= run(64, 128, 32, 1, false, 0, false);
